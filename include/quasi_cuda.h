@@ -1,0 +1,285 @@
+/* quasi_cuda.h - C ABI of libquasi_cuda.so, the GB300 (sm_103a) rendering backend.
+ *
+ * Part 1 declares the host<->plugin boundary that the unchanged Quasi host binds.
+ * It mirrors, with the same member order, types and sizes:
+ *   src/quasi/gpu/types.hpp:14-19   Q_gpu_backend (a uint32_t enum; CUDA is added as value 4)
+ *   src/quasi/gpu/types.hpp:37-42   Q_gpu_context
+ *   src/quasi/gpu/types.hpp:45-50   Q_camera
+ *   src/quasi/gpu/types.hpp:63-70   Q_render_frame
+ *   src/quasi/plugin/plugin_interface.hpp:27-92   handle, version, info, context, readback structs
+ *   src/quasi/plugin/plugin_interface.hpp:107-148 the ten Q_plugin_* entry points
+ * The host resolves these by name with dlsym (src/quasi/plugin/loader.hpp:72-128), so a
+ * plugin built against this header is a drop-in for backends/metal/libquasi_metal.
+ *
+ * Part 2 declares CUDA-only extensions (Q_cuda_*). The reference host never looks them
+ * up; tests, the benchmark and the autograd binding resolve them with dlsym/ctypes.
+ * Every Q_cuda_* call returns an int status: QUASI_OK (0) or a negative QUASI_ERR_*.
+ */
+#ifndef QUASI_CUDA_H
+#define QUASI_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define Q_CUDA_EXPORT __attribute__((visibility("default")))
+#else
+#define Q_CUDA_EXPORT
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ Part 1: plugin ABI */
+
+/* Backend identifier. The reference declares `enum Q_gpu_backend : uint32_t` with values
+ * 0..3 (src/quasi/gpu/types.hpp:14-19); the field stays 4 bytes, CUDA is value 4. */
+typedef uint32_t Q_gpu_backend;
+#define Q_GPU_BACKEND_NONE   0u
+#define Q_GPU_BACKEND_METAL  1u
+#define Q_GPU_BACKEND_VULKAN 2u
+#define Q_GPU_BACKEND_WEBGPU 3u
+#define Q_GPU_BACKEND_CUDA   4u
+
+/* src/quasi/gpu/types.hpp:37-42. For CUDA: device = int* (device ordinal, NULL = 0),
+ * queue = cudaStream_t (NULL = the plugin creates its own stream), layer = NULL. */
+typedef struct Q_gpu_context {
+    Q_gpu_backend backend;
+    void* device;
+    void* queue;
+    void* layer;
+} Q_gpu_context;
+
+/* src/quasi/gpu/types.hpp:45-50 */
+typedef struct Q_camera {
+    float position[3];
+    float target[3];
+    float up[3];
+    float fov; /* vertical field of view, degrees */
+} Q_camera;
+
+/* src/quasi/gpu/types.hpp:63-70. For CUDA: command_buffer = cudaStream_t to render on
+ * (NULL = the plugin's stream); drawable = optional device buffer of width*height RGBA8
+ * pixels that receives the tonemapped image (NULL = no display output, headless). */
+typedef struct Q_render_frame {
+    void* drawable;
+    void* command_buffer;
+    uint32_t width;
+    uint32_t height;
+    Q_camera camera;
+    uint32_t camera_dirty;
+} Q_render_frame;
+
+/* src/quasi/plugin/plugin_interface.hpp:27 */
+typedef struct Q_plugin_handle Q_plugin_handle;
+
+/* src/quasi/plugin/plugin_interface.hpp:30-34 */
+typedef struct Q_plugin_version {
+    uint32_t major;
+    uint32_t minor;
+    uint32_t patch;
+} Q_plugin_version;
+
+/* src/quasi/plugin/plugin_interface.hpp:37-42 */
+typedef struct Q_plugin_info {
+    const char* name;
+    Q_plugin_version version;
+    const char* description;
+    const char* author;
+} Q_plugin_info;
+
+/* src/quasi/plugin/plugin_interface.hpp:48-59 */
+typedef struct Q_plugin_context {
+    uint32_t viewport_width;
+    uint32_t viewport_height;
+    void* host_data;
+    Q_gpu_context* gpu;
+    void (*log)(void* host_data, const char* message);
+    void (*request_shutdown)(void* host_data);
+} Q_plugin_context;
+
+/* src/quasi/plugin/plugin_interface.hpp:65-70. RGBA float, row-major, top row first. */
+typedef struct Q_readback_result {
+    float* data;
+    uint32_t width;
+    uint32_t height;
+    uint32_t channels;
+} Q_readback_result;
+
+/* src/quasi/plugin/plugin_interface.hpp:73-79 (a uint32_t enum in the reference) */
+typedef uint32_t Q_aov_type;
+#define Q_AOV_BEAUTY 0u
+#define Q_AOV_ALBEDO 1u
+#define Q_AOV_NORMAL 2u
+#define Q_AOV_DEPTH  3u
+#define Q_AOV_COUNT  4u
+
+/* src/quasi/plugin/plugin_interface.hpp:82-87 */
+typedef struct Q_aov_buffer {
+    float* data;
+    uint32_t width;
+    uint32_t height;
+    uint32_t channels;
+} Q_aov_buffer;
+
+/* src/quasi/plugin/plugin_interface.hpp:90-92 */
+typedef struct Q_readback_aov_result {
+    Q_aov_buffer buffers[Q_AOV_COUNT];
+} Q_readback_aov_result;
+
+/* Replaces plugin_interface.hpp:108 / plugin.mm:543-545. Returns 3. */
+Q_CUDA_EXPORT uint32_t Q_plugin_abi_version(void);
+/* Replaces plugin_interface.hpp:111 / plugin.mm:547-554. Static strings. */
+Q_CUDA_EXPORT Q_plugin_info Q_plugin_get_info(void);
+/* Replaces plugin_interface.hpp:116 / plugin.mm:556-592. Returns NULL on failure after
+ * logging through ctx->log; requires ctx->gpu->backend == Q_GPU_BACKEND_CUDA. */
+Q_CUDA_EXPORT Q_plugin_handle* Q_plugin_create(Q_plugin_context* ctx);
+/* Replaces plugin_interface.hpp:120 / plugin.mm:594-617. Synchronises and frees all. */
+Q_CUDA_EXPORT void Q_plugin_destroy(Q_plugin_handle* handle);
+/* Replaces plugin_interface.hpp:125 / plugin.mm:619-622 (no-op). */
+Q_CUDA_EXPORT void Q_plugin_update(Q_plugin_handle* handle, float delta_time);
+/* Replaces plugin_interface.hpp:130 / plugin.mm:624-792: one progressive frame. */
+Q_CUDA_EXPORT void Q_plugin_render(Q_plugin_handle* handle, Q_render_frame* frame);
+/* Replaces plugin_interface.hpp:135 / plugin.mm:846-863: malloc'd mean HDR image. */
+Q_CUDA_EXPORT Q_readback_result Q_plugin_readback(Q_plugin_handle* handle);
+/* Replaces plugin_interface.hpp:139 / plugin.mm:865-870. */
+Q_CUDA_EXPORT void Q_plugin_readback_free(Q_readback_result* result);
+/* Replaces plugin_interface.hpp:144 / plugin.mm:872-892: beauty, albedo, normal, depth. */
+Q_CUDA_EXPORT Q_readback_aov_result Q_plugin_readback_aov(Q_plugin_handle* handle);
+/* Replaces plugin_interface.hpp:148 / plugin.mm:894-902. */
+Q_CUDA_EXPORT void Q_plugin_readback_aov_free(Q_readback_aov_result* result);
+
+/* ------------------------------------------------------------ Part 2: CUDA extensions */
+
+#define QUASI_OK              0
+#define QUASI_ERR_INVALID    -1 /* bad argument or unsupported size */
+#define QUASI_ERR_CUDA       -2 /* a CUDA runtime call failed */
+#define QUASI_ERR_OOM        -3 /* device or host allocation failed */
+#define QUASI_ERR_TIMEOUT    -4 /* a bounded device-side wait gave up */
+#define QUASI_ERR_STACK      -5 /* BVH traversal stack would have overflowed */
+#define QUASI_ERR_STATE      -6 /* call made in the wrong state (e.g. no scene) */
+
+/* Integrators. NEE is the triangle/LBVH/next-event path tracer; REFERENCE reproduces the
+ * Metal path_trace loop (plugin.mm:223-276) over quads, brute force, with its seeding. */
+#define QUASI_INTEGRATOR_NEE       0u
+#define QUASI_INTEGRATOR_REFERENCE 1u
+
+/* A scene in host memory, triangles in original order. Arrays are owned by whoever
+ * filled the struct (Q_cuda_make_scene allocates; Q_cuda_free_scene releases). */
+typedef struct Q_cuda_scene {
+    uint32_t tri_count;
+    float* vertices;   /* tri_count * 9: v0.xyz v1.xyz v2.xyz */
+    float* albedo;     /* tri_count * 3 */
+    float* emission;   /* tri_count * 3 */
+    uint32_t quad_count; /* reference-integrator primitives (may be 0) */
+    float* quads;        /* quad_count * 9: origin.xyz u.xyz v.xyz (plugin.mm:57-64) */
+    float* quad_albedo;  /* quad_count * 3 */
+    float* quad_emission;/* quad_count * 3 */
+    Q_camera camera;     /* the scene's own camera */
+} Q_cuda_scene;
+
+/* Render options; zero-initialise and set what you need. A zero field means default. */
+typedef struct Q_cuda_options {
+    uint32_t spp_per_frame;      /* samples per pixel per Q_plugin_render call (1) */
+    uint32_t max_depth;          /* path vertices after the camera (4) */
+    uint32_t seed;               /* RNG seed (0) */
+    uint32_t integrator;         /* QUASI_INTEGRATOR_* */
+    uint32_t rebuild_each_frame; /* rebuild the LBVH in every frame (1 = yes) */
+    uint32_t wave_spp;           /* samples per pixel per wavefront (0 = autotuned) */
+    uint32_t trace_block;        /* threads per block of the trace kernels (0 = auto) */
+    uint32_t record_samples;     /* keep per-sample radiance and path signatures */
+    uint32_t collect_stats;      /* count BVH node visits and triangle tests */
+    uint32_t profile;            /* time every kernel launch with CUDA events */
+    uint32_t megakernel;         /* 1 = one-kernel path tracer instead of the wavefront */
+    uint32_t smem_levels;        /* BVH levels staged in shared memory (0 = default) */
+    float ray_eps;               /* ray origin offset along the normal (1e-4) */
+} Q_cuda_options;
+
+/* Counters of the last frame (rays actually traced) and of the whole accumulation. */
+typedef struct Q_cuda_stats {
+    uint64_t camera_rays;
+    uint64_t extension_rays;  /* closest-hit rays after the camera ray */
+    uint64_t shadow_rays;
+    uint64_t node_visits;     /* only with collect_stats: closest-hit traversal */
+    uint64_t tri_tests;       /* only with collect_stats: closest-hit traversal */
+    uint64_t shadow_node_visits; /* only with collect_stats: any-hit traversal */
+    uint64_t shadow_tri_tests;   /* only with collect_stats: any-hit traversal */
+    uint64_t total_rays;      /* all rays traced since the plugin was created */
+    uint64_t samples_accumulated;
+    uint32_t kernel_launches; /* kernels this library launched in the last frame */
+    uint32_t error_flags;     /* device-side error bits (QUASI_DEVERR_*) */
+    double frame_ms;          /* device time of the last frame (events on the stream) */
+    double bvh_ms;            /* device time of the last LBVH build */
+} Q_cuda_stats;
+
+#define QUASI_DEVERR_STACK     1u
+#define QUASI_DEVERR_TIMEOUT   2u
+#define QUASI_DEVERR_TRAVERSAL 4u /* a traversal or tree climb exceeded its bound */
+
+/* Per-kernel timing from the profile option (one entry per kernel name). */
+typedef struct Q_cuda_kernel_time {
+    char name[48];
+    uint32_t launches;
+    double total_ms;
+} Q_cuda_kernel_time;
+
+/* Builds one of the built-in scenes on the host (no GPU needed). spec is one of
+ *   "cornell36"                 Cornell box of 36 triangles (unit box, camera looking +z)
+ *   "refcornell"                src/quasi/scene/cornell_box.hpp:95-134 as 32 triangles + 16 quads
+ *   "soup:n=<N>,seed=<S>"       seeded random triangle soup, 1% emitters
+ * Returns QUASI_OK and fills *out; free with Q_cuda_free_scene. */
+Q_CUDA_EXPORT int Q_cuda_make_scene(const char* spec, Q_cuda_scene* out);
+Q_CUDA_EXPORT void Q_cuda_free_scene(Q_cuda_scene* scene);
+
+/* Replaces the plugin's scene (copied to the device; the host arrays may be freed). */
+Q_CUDA_EXPORT int Q_cuda_set_scene(Q_plugin_handle* handle, const Q_cuda_scene* scene);
+/* Updates triangle vertices in place (same count); the next frame rebuilds the LBVH. */
+Q_CUDA_EXPORT int Q_cuda_update_vertices(Q_plugin_handle* handle, const float* vertices,
+                                         uint32_t tri_count);
+/* Replaces per-triangle materials (host arrays, tri_count*3 each); resets accumulation. */
+Q_CUDA_EXPORT int Q_cuda_set_materials(Q_plugin_handle* handle, const float* albedo,
+                                       const float* emission, uint32_t tri_count);
+Q_CUDA_EXPORT int Q_cuda_set_options(Q_plugin_handle* handle, const Q_cuda_options* options);
+Q_CUDA_EXPORT int Q_cuda_get_options(Q_plugin_handle* handle, Q_cuda_options* options);
+/* Clears the accumulation (next frame starts at sample 0). */
+Q_CUDA_EXPORT int Q_cuda_reset(Q_plugin_handle* handle);
+/* Waits for the plugin's stream; returns the first pending error, if any. */
+Q_CUDA_EXPORT int Q_cuda_synchronize(Q_plugin_handle* handle);
+Q_CUDA_EXPORT int Q_cuda_get_stats(Q_plugin_handle* handle, Q_cuda_stats* stats);
+/* Copies up to capacity per-kernel timing entries; *count receives how many exist. */
+Q_CUDA_EXPORT int Q_cuda_kernel_times(Q_plugin_handle* handle, Q_cuda_kernel_time* out,
+                                      uint32_t capacity, uint32_t* count);
+Q_CUDA_EXPORT const char* Q_cuda_last_error(Q_plugin_handle* handle);
+
+/* Copies the current LBVH to host arrays (any pointer may be NULL). n = tri_count.
+ *   morton    [n]        30-bit Morton code per triangle, original order
+ *   order     [n]        original triangle index of each sorted position
+ *   children  [2*(n-1)]  per internal node: child >= 0 internal node, child < 0 leaf ~pos
+ *   boxes     [12*(n-1)] per internal node: child0 lo.xyz hi.xyz, child1 lo.xyz hi.xyz
+ *   bounds    [6]        centroid bounds lo.xyz hi.xyz used for quantisation */
+Q_CUDA_EXPORT int Q_cuda_read_bvh(Q_plugin_handle* handle, uint32_t* morton, uint32_t* order,
+                                  int32_t* children, float* boxes, float* bounds);
+
+/* With record_samples: copies the last frame's per-sample radiance (width*height*spp*3,
+ * ordered pixel-major then sample) and path signatures (width*height*spp). */
+Q_CUDA_EXPORT int Q_cuda_read_samples(Q_plugin_handle* handle, float* radiance,
+                                      uint32_t* signatures);
+
+/* Writes the mean HDR image (RGBA float) into a caller-provided device pointer. */
+Q_CUDA_EXPORT int Q_cuda_resolve_device(Q_plugin_handle* handle, float* device_rgba);
+
+/* Sorts n (key, value) pairs in place on the device with the library's LSD radix sort
+ * (stable; keys compared as unsigned 32-bit over bits [0, key_bits)). Device pointers. */
+Q_CUDA_EXPORT int Q_cuda_radix_sort_pairs(uint32_t* device_keys, uint32_t* device_values,
+                                          uint32_t n, uint32_t key_bits, void* stream);
+
+/* Runs the autotuner on the current scene/options and stores the result in the options
+ * (wave_spp, trace_block). budget_ms bounds the time spent. */
+Q_CUDA_EXPORT int Q_cuda_autotune(Q_plugin_handle* handle, double budget_ms);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* QUASI_CUDA_H */

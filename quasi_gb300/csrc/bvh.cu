@@ -1,0 +1,476 @@
+// bvh.cu - GPU LBVH construction: centroid bounds, Morton-30 codes, stable LSD radix sort,
+// Karras (2012) hierarchy and bottom-up child boxes. All FP32 arithmetic feeding integer
+// results uses round-to-nearest intrinsics so the compiler cannot contract it, which keeps
+// Morton codes, the sort order and the topology bit-exact against the oracle.
+#include "bvh.cuh"
+#include "common.cuh"
+
+#include <algorithm>
+#include <cfloat>
+#include <cstring>
+#include <vector>
+
+namespace quasi {
+namespace {
+
+constexpr int k_sort_block = 256;
+constexpr int k_sort_items = 8;
+constexpr int k_sort_tile = k_sort_block * k_sort_items;
+constexpr int k_sort_warps = k_sort_block / 32;
+
+// ---------------------------------------------------------------- radix sort (8-bit digits)
+
+__global__ void __launch_bounds__(k_sort_block)
+k_radix_hist(const uint32_t* __restrict__ keys, uint32_t n, int shift, uint32_t* __restrict__ hist,
+             uint32_t nblocks) {
+    __shared__ uint32_t h[256];
+    for (int i = threadIdx.x; i < 256; i += k_sort_block) h[i] = 0;
+    __syncthreads();
+    const uint32_t base = blockIdx.x * k_sort_tile;
+#pragma unroll
+    for (int r = 0; r < k_sort_items; ++r) {
+        const uint32_t i = base + r * k_sort_block + threadIdx.x;
+        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < 256; d += k_sort_block) hist[d * nblocks + blockIdx.x] = h[d];
+}
+
+// Exclusive scan of m entries in one block of 1024 threads (m is at most a few million).
+__global__ void __launch_bounds__(1024) k_scan_exclusive(uint32_t* data, uint32_t m) {
+    __shared__ uint32_t warp_sums[32];
+    const uint32_t per = (m + 1023u) / 1024u;
+    const uint32_t begin = min(threadIdx.x * per, m);
+    const uint32_t end = min(begin + per, m);
+    uint32_t sum = 0;
+    for (uint32_t i = begin; i < end; ++i) sum += data[i];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t v = warp_sums[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += y;
+        }
+        warp_sums[lane] = v;
+    }
+    __syncthreads();
+    uint32_t prefix = x - sum + (warp > 0 ? warp_sums[warp - 1] : 0u);
+    for (uint32_t i = begin; i < end; ++i) {
+        const uint32_t t = data[i];
+        data[i] = prefix;
+        prefix += t;
+    }
+}
+
+// Stable scatter. Warp w of a block owns the contiguous sub-tile [w*256, (w+1)*256) of the
+// block's 2048 keys and walks it in 8 rounds of 32; ranks inside a round come from
+// __match_any_sync, ranks across rounds from per-warp digit counters, and ranks across
+// warps from a per-digit prefix over the warps' counters.
+__global__ void __launch_bounds__(k_sort_block)
+k_radix_scatter(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+                uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n, int shift,
+                const uint32_t* __restrict__ hist, uint32_t nblocks) {
+    __shared__ uint32_t warp_cnt[k_sort_warps][256];
+    __shared__ uint32_t block_off[256];
+    for (int i = threadIdx.x; i < k_sort_warps * 256; i += k_sort_block) (&warp_cnt[0][0])[i] = 0;
+    for (int d = threadIdx.x; d < 256; d += k_sort_block) block_off[d] = hist[d * nblocks + blockIdx.x];
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t lt = lanemask_lt();
+    const uint32_t warp_base = blockIdx.x * k_sort_tile + warp * 32 * k_sort_items;
+    uint32_t key[k_sort_items], val[k_sort_items], rank[k_sort_items];
+#pragma unroll
+    for (int r = 0; r < k_sort_items; ++r) {
+        const uint32_t i = warp_base + r * 32 + lane;
+        const bool valid = i < n;
+        key[r] = valid ? keys_in[i] : 0u;
+        val[r] = valid ? vals_in[i] : 0u;
+        const uint32_t d = (key[r] >> shift) & 255u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 256u + lane);
+        const uint32_t before = __popc(peers & lt);
+        uint32_t cnt = 0;
+        if (valid) cnt = warp_cnt[warp][d];
+        __syncwarp();
+        if (valid && before == 0) warp_cnt[warp][d] = cnt + __popc(peers);
+        __syncwarp();
+        rank[r] = valid ? cnt + before : 0xffffffffu;
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < 256; d += k_sort_block) {
+        uint32_t run = 0;
+#pragma unroll
+        for (int w = 0; w < k_sort_warps; ++w) {
+            const uint32_t c = warp_cnt[w][d];
+            warp_cnt[w][d] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < k_sort_items; ++r) {
+        if (rank[r] == 0xffffffffu) continue;
+        const uint32_t d = (key[r] >> shift) & 255u;
+        const uint32_t pos = block_off[d] + warp_cnt[warp][d] + rank[r];
+        keys_out[pos] = key[r];
+        vals_out[pos] = val[r];
+    }
+}
+
+// ---------------------------------------------------------------- bounds and Morton codes
+
+__device__ __forceinline__ float3 centroid(float4 a, float4 b, float4 c) {
+    const float third = 1.0f / 3.0f;
+    return mk3(__fmul_rn(__fadd_rn(__fadd_rn(a.x, b.x), c.x), third),
+               __fmul_rn(__fadd_rn(__fadd_rn(a.y, b.y), c.y), third),
+               __fmul_rn(__fadd_rn(__fadd_rn(a.z, b.z), c.z), third));
+}
+
+__device__ __forceinline__ float warp_min(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__global__ void __launch_bounds__(256) k_bounds_partial(const float4* __restrict__ tri, uint32_t n,
+                                                        float* __restrict__ partial) {
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float3 c = centroid(__ldg(&tri[3 * i]), __ldg(&tri[3 * i + 1]), __ldg(&tri[3 * i + 2]));
+        lo[0] = fminf(lo[0], c.x); lo[1] = fminf(lo[1], c.y); lo[2] = fminf(lo[2], c.z);
+        hi[0] = fmaxf(hi[0], c.x); hi[1] = fmaxf(hi[1], c.y); hi[2] = fmaxf(hi[2], c.z);
+    }
+    __shared__ float s[8][6];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { lo[a] = warp_min(lo[a]); hi[a] = warp_max(hi[a]); }
+    if (lane == 0) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) { s[warp][a] = lo[a]; s[warp][3 + a] = hi[a]; }
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        float v = s[0][threadIdx.x];
+        for (int w = 1; w < 8; ++w) v = threadIdx.x < 3 ? fminf(v, s[w][threadIdx.x]) : fmaxf(v, s[w][threadIdx.x]);
+        partial[blockIdx.x * 6 + threadIdx.x] = v;
+    }
+}
+
+__global__ void k_bounds_final(const float* __restrict__ partial, int nparts, float* __restrict__ bounds) {
+    const int lane = threadIdx.x;
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int p = lane; p < nparts; p += 32) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = fminf(lo[a], partial[p * 6 + a]);
+            hi[a] = fmaxf(hi[a], partial[p * 6 + 3 + a]);
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { lo[a] = warp_min(lo[a]); hi[a] = warp_max(hi[a]); }
+    if (lane == 0) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            bounds[a] = lo[a];
+            bounds[3 + a] = hi[a];
+            const float ext = __fsub_rn(hi[a], lo[a]);
+            bounds[6 + a] = ext > 0.0f ? __fdiv_rn(1.0f, ext) : 0.0f;
+        }
+        bounds[9] = bounds[10] = bounds[11] = 0.0f;
+    }
+}
+
+// Spreads the low 10 bits of v to every third bit (bit k -> bit 3k).
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+
+__device__ __forceinline__ uint32_t quantize10(float c, float lo, float inv) {
+    const float q = fminf(fmaxf(__fmul_rn(__fmul_rn(__fsub_rn(c, lo), inv), 1024.0f), 0.0f), 1023.0f);
+    return static_cast<uint32_t>(q);
+}
+
+__global__ void __launch_bounds__(256) k_morton(const float4* __restrict__ tri, uint32_t n,
+                                                const float* __restrict__ bounds, uint32_t* __restrict__ morton,
+                                                uint32_t* __restrict__ keys, uint32_t* __restrict__ order) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float3 c = centroid(__ldg(&tri[3 * i]), __ldg(&tri[3 * i + 1]), __ldg(&tri[3 * i + 2]));
+    const uint32_t qx = quantize10(c.x, bounds[0], bounds[6]);
+    const uint32_t qy = quantize10(c.y, bounds[1], bounds[7]);
+    const uint32_t qz = quantize10(c.z, bounds[2], bounds[8]);
+    const uint32_t code = (spread3(qx) << 2) | (spread3(qy) << 1) | spread3(qz);
+    morton[i] = code;
+    keys[i] = code;
+    order[i] = i;
+}
+
+// ---------------------------------------------------------------- Karras hierarchy
+
+// Common-prefix length of sorted keys i and j, index-augmented for equal keys; -1 outside.
+__device__ __forceinline__ int prefix_len(const uint32_t* __restrict__ keys, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    const uint32_t a = __ldg(&keys[i]), b = __ldg(&keys[j]);
+    if (a == b) return 32 + __clz(i ^ j);
+    return __clz(a ^ b);
+}
+
+__global__ void __launch_bounds__(256) k_karras(const uint32_t* __restrict__ keys, int n,
+                                                float4* __restrict__ nodes, int* __restrict__ parent) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const int dl = prefix_len(keys, n, i, i - 1);
+    const int dr = prefix_len(keys, n, i, i + 1);
+    const int d = dr > dl ? 1 : -1;
+    const int dmin = min(dl, dr);
+    int lmax = 2;
+    while (prefix_len(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (prefix_len(keys, n, i, i + (l + t) * d) > dmin) l += t;
+    const int j = i + l * d;
+    const int dnode = prefix_len(keys, n, i, j);
+    int s = 0, t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (prefix_len(keys, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    const int gamma = i + s * d + min(d, 0);
+    const int left = (min(i, j) == gamma) ? ~gamma : gamma;
+    const int right = (max(i, j) == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+    nodes[4 * i + 3] = make_float4(__int_as_float(left), __int_as_float(right), 0.f, 0.f);
+    parent[left >= 0 ? left : (n - 1) + ~left] = i;
+    parent[right >= 0 ? right : (n - 1) + ~right] = i;
+    if (i == 0) parent[0] = -1;
+}
+
+// One thread per leaf: gathers the triangle into leaf order and climbs to the root,
+// writing each child's box into its parent's slot. The second thread to arrive at a node
+// (arrival counter) owns the union and continues upwards.
+__global__ void __launch_bounds__(256) k_leaf_boxes(const float4* __restrict__ tri_in,
+                                                    const uint32_t* __restrict__ order, int n,
+                                                    const int* __restrict__ parent, float4* nodes,
+                                                    uint32_t* flags, float4* __restrict__ tris,
+                                                    uint32_t* __restrict__ err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t o = order[i];
+    const float4 a = __ldg(&tri_in[3 * o]), b = __ldg(&tri_in[3 * o + 1]), c = __ldg(&tri_in[3 * o + 2]);
+    tris[3 * i] = make_float4(a.x, a.y, a.z, __int_as_float(static_cast<int>(o)));
+    tris[3 * i + 1] = make_float4(__fsub_rn(b.x, a.x), __fsub_rn(b.y, a.y), __fsub_rn(b.z, a.z), 0.f);
+    tris[3 * i + 2] = make_float4(__fsub_rn(c.x, a.x), __fsub_rn(c.y, a.y), __fsub_rn(c.z, a.z), 0.f);
+    float3 lo = mk3(fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z)));
+    float3 hi = mk3(fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z)));
+    if (n == 1) {
+        nodes[0] = make_float4(lo.x, hi.x, lo.y, hi.y);
+        nodes[1] = make_float4(lo.x, hi.x, lo.y, hi.y);
+        nodes[2] = make_float4(lo.z, hi.z, lo.z, hi.z);
+        nodes[3] = make_float4(__int_as_float(~0), __int_as_float(~0), 0.f, 0.f);
+        return;
+    }
+    int child = ~i;
+    int p = parent[(n - 1) + i];
+    // Depth is bounded by the 64 bits of the index-augmented keys; a longer climb means a
+    // malformed parent array.
+    for (int depth = 0;; ++depth) {
+        if (depth > 128 || p < 0 || p >= n - 1) {
+            atomicOr(err, k_deverr_traversal);
+            return;
+        }
+        const float4 meta = __ldcg(&nodes[4 * p + 3]);
+        const int slot = (__float_as_int(meta.x) == child) ? 0 : 1;
+        nodes[4 * p + slot] = make_float4(lo.x, hi.x, lo.y, hi.y);
+        reinterpret_cast<float2*>(&nodes[4 * p + 2])[slot] = make_float2(lo.z, hi.z);
+        __threadfence();
+        if (atomicAdd(&flags[p], 1u) == 0u) return;
+        __threadfence();
+        const float4 n0 = __ldcg(&nodes[4 * p]);
+        const float4 n1 = __ldcg(&nodes[4 * p + 1]);
+        const float4 n2 = __ldcg(&nodes[4 * p + 2]);
+        lo = mk3(fminf(n0.x, n1.x), fminf(n0.z, n1.z), fminf(n2.x, n2.z));
+        hi = mk3(fmaxf(n0.y, n1.y), fmaxf(n0.w, n1.w), fmaxf(n2.y, n2.w));
+        if (p == 0) return;
+        child = p;
+        p = parent[p];
+    }
+}
+
+inline uint32_t ceil_div(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
+
+}  // namespace
+
+// ---------------------------------------------------------------- host: radix sort
+
+size_t radix_sort_hist_entries(uint32_t n) { return 256ull * ceil_div(n > 0 ? n : 1, k_sort_tile); }
+
+cudaError_t radix_sort_reserve(RadixSortScratch& s, uint32_t n) {
+    if (n <= s.capacity && radix_sort_hist_entries(n) <= s.hist_capacity) return cudaSuccess;
+    radix_sort_release(s);
+    QUASI_TRY_CUDA(cudaMalloc(&s.keys_alt, sizeof(uint32_t) * std::max<uint32_t>(n, 1)));
+    QUASI_TRY_CUDA(cudaMalloc(&s.vals_alt, sizeof(uint32_t) * std::max<uint32_t>(n, 1)));
+    const size_t h = radix_sort_hist_entries(n);
+    QUASI_TRY_CUDA(cudaMalloc(&s.hist, sizeof(uint32_t) * h));
+    s.capacity = n;
+    s.hist_capacity = static_cast<uint32_t>(h);
+    return cudaSuccess;
+}
+
+void radix_sort_release(RadixSortScratch& s) {
+    if (s.keys_alt) cudaFree(s.keys_alt);
+    if (s.vals_alt) cudaFree(s.vals_alt);
+    if (s.hist) cudaFree(s.hist);
+    s = RadixSortScratch{};
+}
+
+cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t n, int key_bits,
+                             RadixSortScratch& s, cudaStream_t stream, KernelProfiler& prof) {
+    if (n <= 1) return cudaSuccess;
+    if (n > s.capacity) return cudaErrorInvalidValue;
+    const uint32_t nblocks = ceil_div(n, k_sort_tile);
+    const int passes = (key_bits + 7) / 8;
+    uint32_t *ki = keys, *vi = vals, *ko = s.keys_alt, *vo = s.vals_alt;
+    for (int p = 0; p < passes; ++p) {
+        const int shift = 8 * p;
+        QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "radix_hist", stream,
+                                    (k_radix_hist<<<nblocks, k_sort_block, 0, stream>>>(ki, n, shift, s.hist, nblocks))));
+        QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "radix_scan", stream,
+                                    (k_scan_exclusive<<<1, 1024, 0, stream>>>(s.hist, 256u * nblocks))));
+        QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "radix_scatter", stream,
+                                    (k_radix_scatter<<<nblocks, k_sort_block, 0, stream>>>(ki, vi, ko, vo, n, shift,
+                                                                                           s.hist, nblocks))));
+        std::swap(ki, ko);
+        std::swap(vi, vo);
+    }
+    if (ki != keys) {
+        QUASI_TRY_CUDA(cudaMemcpyAsync(keys, ki, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, stream));
+        QUASI_TRY_CUDA(cudaMemcpyAsync(vals, vi, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, stream));
+    }
+    return cudaSuccess;
+}
+
+// ---------------------------------------------------------------- host: LBVH builder
+
+cudaError_t LbvhBuilder::reserve(uint32_t n) {
+    if (n <= capacity_ && bounds_) return cudaSuccess;
+    release();
+    const uint32_t m = std::max<uint32_t>(n, 2);
+    QUASI_TRY_CUDA(cudaMalloc(&bounds_, sizeof(float) * 12));
+    QUASI_TRY_CUDA(cudaMalloc(&partial_, sizeof(float) * 6 * k_bounds_blocks));
+    QUASI_TRY_CUDA(cudaMalloc(&morton_, sizeof(uint32_t) * m));
+    QUASI_TRY_CUDA(cudaMalloc(&keys_, sizeof(uint32_t) * m));
+    QUASI_TRY_CUDA(cudaMalloc(&order_, sizeof(uint32_t) * m));
+    QUASI_TRY_CUDA(cudaMalloc(&parent_, sizeof(int) * (2 * m)));
+    QUASI_TRY_CUDA(cudaMalloc(&flags_, sizeof(uint32_t) * m));
+    QUASI_TRY_CUDA(cudaMalloc(&nodes_, sizeof(float4) * 4 * m));
+    QUASI_TRY_CUDA(cudaMalloc(&tris_, sizeof(float4) * 3 * m));
+    QUASI_TRY_CUDA(radix_sort_reserve(sort_, m));
+    capacity_ = m;
+    return cudaSuccess;
+}
+
+void LbvhBuilder::release() {
+    for (void* p : {static_cast<void*>(bounds_), static_cast<void*>(partial_), static_cast<void*>(morton_),
+                    static_cast<void*>(keys_), static_cast<void*>(order_), static_cast<void*>(parent_),
+                    static_cast<void*>(flags_), static_cast<void*>(nodes_), static_cast<void*>(tris_)})
+        if (p) cudaFree(p);
+    bounds_ = partial_ = nullptr;
+    morton_ = keys_ = order_ = flags_ = nullptr;
+    parent_ = nullptr;
+    nodes_ = tris_ = nullptr;
+    radix_sort_release(sort_);
+    capacity_ = 0;
+    n_ = 0;
+}
+
+cudaError_t LbvhBuilder::build(const float4* tri_in, uint32_t n, cudaStream_t stream, KernelProfiler& prof,
+                               uint32_t* err) {
+    QUASI_TRY_CUDA(reserve(n));
+    n_ = n;
+    if (n == 0) return cudaSuccess;
+    const int parts = static_cast<int>(std::min<uint32_t>(k_bounds_blocks, ceil_div(n, 256)));
+    QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_bounds", stream,
+                                (k_bounds_partial<<<parts, 256, 0, stream>>>(tri_in, n, partial_))));
+    QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_bounds_final", stream,
+                                (k_bounds_final<<<1, 32, 0, stream>>>(partial_, parts, bounds_))));
+    QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_morton", stream,
+                                (k_morton<<<ceil_div(n, 256), 256, 0, stream>>>(tri_in, n, bounds_, morton_, keys_,
+                                                                                order_))));
+    QUASI_TRY_CUDA(radix_sort_pairs(keys_, order_, n, 30, sort_, stream, prof));
+    if (n > 1) {
+        QUASI_TRY_CUDA(cudaMemsetAsync(flags_, 0, sizeof(uint32_t) * (n - 1), stream));
+        QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_karras", stream,
+                                    (k_karras<<<ceil_div(n - 1, 256), 256, 0, stream>>>(keys_, static_cast<int>(n),
+                                                                                        nodes_, parent_))));
+    }
+    QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_leaf_boxes", stream,
+                                (k_leaf_boxes<<<ceil_div(n, 256), 256, 0, stream>>>(
+                                    tri_in, order_, static_cast<int>(n), parent_, nodes_, flags_, tris_, err))));
+    return cudaSuccess;
+}
+
+cudaError_t LbvhBuilder::read(uint32_t* morton, uint32_t* order, int32_t* children, float* boxes, float* bounds,
+                              cudaStream_t stream) const {
+    QUASI_TRY_CUDA(cudaStreamSynchronize(stream));
+    if (n_ == 0) return cudaSuccess;
+    if (morton) QUASI_TRY_CUDA(cudaMemcpy(morton, morton_, sizeof(uint32_t) * n_, cudaMemcpyDeviceToHost));
+    if (order) QUASI_TRY_CUDA(cudaMemcpy(order, order_, sizeof(uint32_t) * n_, cudaMemcpyDeviceToHost));
+    if (bounds) QUASI_TRY_CUDA(cudaMemcpy(bounds, bounds_, sizeof(float) * 6, cudaMemcpyDeviceToHost));
+    const uint32_t nodes = n_ > 1 ? n_ - 1 : 1;
+    if (children || boxes) {
+        std::vector<float4> host(4 * nodes);
+        QUASI_TRY_CUDA(cudaMemcpy(host.data(), nodes_, sizeof(float4) * 4 * nodes, cudaMemcpyDeviceToHost));
+        for (uint32_t i = 0; i < nodes; ++i) {
+            const float4 n0 = host[4 * i], n1 = host[4 * i + 1], n2 = host[4 * i + 2], n3 = host[4 * i + 3];
+            if (children) {
+                int32_t c0, c1;
+                std::memcpy(&c0, &n3.x, 4);
+                std::memcpy(&c1, &n3.y, 4);
+                children[2 * i] = c0;
+                children[2 * i + 1] = c1;
+            }
+            if (boxes) {
+                float* b = boxes + 12 * i;
+                b[0] = n0.x; b[1] = n0.z; b[2] = n2.x; b[3] = n0.y; b[4] = n0.w; b[5] = n2.y;
+                b[6] = n1.x; b[7] = n1.z; b[8] = n2.z; b[9] = n1.y; b[10] = n1.w; b[11] = n2.w;
+            }
+        }
+    }
+    return cudaSuccess;
+}
+
+}  // namespace quasi
+
+// Standalone sort entry point (allocates its own scratch for the call).
+extern "C" __attribute__((visibility("default"))) int Q_cuda_radix_sort_pairs(uint32_t* device_keys,
+                                                                              uint32_t* device_values, uint32_t n,
+                                                                              uint32_t key_bits, void* stream) {
+    if (n == 0) return 0;
+    if (!device_keys || !device_values || key_bits == 0 || key_bits > 32) return -1;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    quasi::RadixSortScratch scratch;
+    quasi::KernelProfiler prof;
+    cudaError_t e = quasi::radix_sort_reserve(scratch, n);
+    if (e == cudaSuccess) e = quasi::radix_sort_pairs(device_keys, device_values, n, static_cast<int>(key_bits), scratch, s, prof);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    quasi::radix_sort_release(scratch);
+    return e == cudaSuccess ? 0 : (e == cudaErrorMemoryAllocation ? -3 : -2);
+}

@@ -1,0 +1,87 @@
+// bvh.cuh - linear BVH (LBVH) built on the GPU every frame.
+//
+// Pipeline (one scene of n triangles, all integer steps bit-exact against the oracle):
+//   1. centroid bounds   c = ((v0 + v1) + v2) * (1/3) in FP32, min/max reduction
+//   2. Morton-30 codes    q = min(max((c - lo) * (1/(hi - lo)) * 1024, 0), 1023) per axis,
+//                         code = (expand(qx) << 2) | (expand(qy) << 1) | expand(qz)
+//   3. stable LSD radix sort of (code, index) on 8-bit digits
+//   4. Karras 2012 hierarchy (index-augmented common-prefix for duplicate codes)
+//   5. bottom-up child boxes with per-node arrival counters; triangles gathered into
+//      leaf order as {v0, orig index}, {e1}, {e2}
+//
+// Node layout, 64 bytes (4 x float4), child boxes stored in the parent:
+//   n0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
+//   n1 = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
+//   n2 = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
+//   n3 = (child0, child1, 0, 0) as ints; child >= 0 internal node, child < 0 leaf ~pos.
+// A scene of one triangle gets a single node whose second child has an empty box.
+#pragma once
+
+#include "launch.hpp"
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace quasi {
+
+// Sorts (keys, values) by the low key_bits of keys; stable. keys/values and the alt
+// buffers are swapped internally; on return the sorted data is in keys/values.
+struct RadixSortScratch {
+    uint32_t* keys_alt = nullptr;
+    uint32_t* vals_alt = nullptr;
+    uint32_t* hist = nullptr;
+    uint32_t capacity = 0;
+    uint32_t hist_capacity = 0;
+};
+
+size_t radix_sort_hist_entries(uint32_t n);
+cudaError_t radix_sort_reserve(RadixSortScratch& s, uint32_t n);
+void radix_sort_release(RadixSortScratch& s);
+cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t n, int key_bits,
+                             RadixSortScratch& s, cudaStream_t stream, KernelProfiler& prof);
+
+struct LbvhView {
+    const float4* nodes = nullptr;  // 4 float4 per internal node
+    const float4* tris = nullptr;   // 3 float4 per triangle in leaf order
+    uint32_t tri_count = 0;
+    uint32_t node_count = 0;
+};
+
+class LbvhBuilder {
+public:
+    LbvhBuilder() = default;
+    ~LbvhBuilder() { release(); }
+    LbvhBuilder(const LbvhBuilder&) = delete;
+    LbvhBuilder& operator=(const LbvhBuilder&) = delete;
+
+    cudaError_t reserve(uint32_t n);
+    void release();
+
+    // tri_in: 3 float4 per triangle (v0, v1, v2; w ignored), original order, device.
+    // err: device word that receives QUASI_DEVERR_* bits if the hierarchy is malformed.
+    cudaError_t build(const float4* tri_in, uint32_t n, cudaStream_t stream, KernelProfiler& prof, uint32_t* err);
+
+    LbvhView view() const { return LbvhView{nodes_, tris_, n_, n_ == 0 ? 0u : (n_ > 1 ? n_ - 1 : 1u)}; }
+
+    // Debug copies to host (stream-synchronous).
+    cudaError_t read(uint32_t* morton, uint32_t* order, int32_t* children, float* boxes,
+                     float* bounds, cudaStream_t stream) const;
+
+private:
+    uint32_t n_ = 0;
+    uint32_t capacity_ = 0;
+    float* bounds_ = nullptr;        // 12 floats: lo.xyz hi.xyz inv.xyz pad
+    float* partial_ = nullptr;       // per-block partial bounds
+    uint32_t* morton_ = nullptr;     // original order
+    uint32_t* keys_ = nullptr;       // sorted keys
+    uint32_t* order_ = nullptr;      // sorted original indices
+    int* parent_ = nullptr;          // [n-1 internal][n leaves]
+    uint32_t* flags_ = nullptr;      // arrival counters, n-1
+    float4* nodes_ = nullptr;
+    float4* tris_ = nullptr;
+    RadixSortScratch sort_;
+};
+
+constexpr int k_bounds_blocks = 304;  // 2 x 152 SMs
+
+}  // namespace quasi

@@ -1,0 +1,90 @@
+// launch.hpp - kernel launch bookkeeping: error checks, a launch counter and optional
+// per-kernel CUDA-event timing on the launching stream.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <map>
+#include <string>
+#include <vector>
+
+namespace quasi {
+
+class KernelProfiler {
+public:
+    ~KernelProfiler() {
+        for (auto& r : pending_) { pool_.push_back(r.a); pool_.push_back(r.b); }
+        for (cudaEvent_t e : pool_) cudaEventDestroy(e);
+    }
+
+    void set_enabled(bool on) { enabled_ = on; }
+    bool enabled() const { return enabled_; }
+
+    // Brackets one launch on `stream`; returns false if an event could not be created.
+    void begin(const char* name, cudaStream_t stream) {
+        ++launches_;
+        if (!enabled_) return;
+        Rec r{name, take(), take()};
+        if (r.a && r.b) cudaEventRecord(r.a, stream);
+        pending_.push_back(r);
+    }
+    void end(cudaStream_t stream) {
+        if (!enabled_ || pending_.empty()) return;
+        Rec& r = pending_.back();
+        if (r.a && r.b) cudaEventRecord(r.b, stream);
+    }
+
+    // Call after the stream has been synchronised: folds pending events into totals.
+    void collect() {
+        for (auto& r : pending_) {
+            float ms = 0.f;
+            if (r.a && r.b && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+                auto& t = totals_[r.name];
+                t.first += 1;
+                t.second += ms;
+            }
+            if (r.a) pool_.push_back(r.a);
+            if (r.b) pool_.push_back(r.b);
+        }
+        pending_.clear();
+    }
+
+    void reset_totals() { totals_.clear(); }
+    uint32_t launches() const { return launches_; }
+    void reset_launches() { launches_ = 0; }
+    const std::map<std::string, std::pair<uint32_t, double>>& totals() const { return totals_; }
+
+private:
+    struct Rec { const char* name; cudaEvent_t a; cudaEvent_t b; };
+    cudaEvent_t take() {
+        if (!pool_.empty()) { cudaEvent_t e = pool_.back(); pool_.pop_back(); return e; }
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        return e;
+    }
+    bool enabled_ = false;
+    uint32_t launches_ = 0;
+    std::vector<Rec> pending_;
+    std::vector<cudaEvent_t> pool_;
+    std::map<std::string, std::pair<uint32_t, double>> totals_;
+};
+
+}  // namespace quasi
+
+// Launches `call` (a <<<>>> expression) on `stream`, counting and optionally timing it.
+// Evaluates to a cudaError_t from cudaGetLastError().
+#define QUASI_LAUNCH(prof, name, stream, call) \
+    ([&]() -> cudaError_t {                    \
+        (prof).begin(name, stream);            \
+        call;                                  \
+        (prof).end(stream);                    \
+        return cudaGetLastError();             \
+    }())
+
+#define QUASI_TRY_CUDA(expr)                                       \
+    do {                                                           \
+        cudaError_t quasi_err_ = (expr);                           \
+        if (quasi_err_ != cudaSuccess) return quasi_err_;          \
+    } while (0)

@@ -1,0 +1,229 @@
+"""GPU path tracer parity against the FP64 oracle at matched seeds.
+
+Tolerance: per-pixel relative error |gpu - oracle| / max(|oracle|, 1e-3) <= 1e-4 for every
+pixel whose path signatures (the sequence of triangles hit and shadow-ray outcomes) all
+agree with the oracle's. A path whose FP32 branch decision differs from FP64 (a ray grazing
+an edge) is counted as divergent; divergent pixels must stay rare.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import quasi_gb300 as q
+
+pytestmark = pytest.mark.gpu
+
+REL_TOL = 1e-4
+FLOOR = 1e-3
+
+
+@pytest.fixture(scope="module")
+def host(cuda_ok):
+    h = q.PluginHost(width=64, height=64)
+    yield h
+    h.destroy()
+
+
+def _render(host, scene, w, h, spp, depth, seed=0, frames=1, **opts):
+    host.set_scene(scene)
+    host.set_options(spp_per_frame=spp, max_depth=depth, seed=seed, record_samples=1, **opts)
+    for f in range(frames):
+        host.render(w, h, dirty=(f == 0))
+    img = host.readback()
+    rad, sig = host.read_samples(spp)
+    st = host.stats()
+    assert st.error_flags == 0, st.error_flags
+    return img, rad, sig, st
+
+
+def _rel(a, b):
+    return np.abs(a - b) / np.maximum(np.abs(b), FLOOR)
+
+
+def _check_parity(img, rad, sig, ref, w, h, spp, max_divergent=1e-3):
+    osig = ref["sig"].reshape(h, w, spp)
+    osamp = ref["samples"].reshape(h, w, spp, 3)
+    match = sig == osig
+    # per sample, on agreeing paths
+    s_err = _rel(rad.astype(np.float64), osamp).max(-1)
+    assert s_err[match].max() <= REL_TOL, s_err[match].max()
+    # per pixel, on pixels whose paths all agree
+    px_ok = match.all(-1)
+    p_err = _rel(img[..., :3].astype(np.float64), ref["mean"].reshape(h, w, 3)).max(-1)
+    assert p_err[px_ok].max() <= REL_TOL, p_err[px_ok].max()
+    assert 1.0 - px_ok.mean() <= max_divergent, 1.0 - px_ok.mean()
+    return p_err, px_ok
+
+
+def test_cornell36_parity(host, orc):
+    """Cornell box of 36 triangles, 256x256, 16 spp, depth 4, seed 0."""
+    w = h = 256
+    spp, depth = 16, 4
+    scene = q.make_scene("cornell36", host.lib)
+    img, rad, sig, st = _render(host, scene, w, h, spp, depth)
+    ref = orc.render_nee(scene, w, h, spp, depth, seed=0, want_samples=True)
+    _check_parity(img, rad, sig, ref, w, h, spp)
+    assert st.camera_rays == w * h * spp
+    # ray counts agree with the oracle up to the divergent paths
+    for k, v in (("camera", st.camera_rays), ("extension", st.extension_rays), ("shadow", st.shadow_rays)):
+        assert abs(int(v) - ref["rays"][k]) <= 1e-3 * ref["rays"][k] + 8, (k, v, ref["rays"][k])
+
+
+def test_refcornell_triangles_parity(host, orc):
+    """The reference's own Cornell scene (cornell_box.hpp) as 32 triangles, NEE integrator."""
+    w, h = 96, 72
+    spp, depth = 8, 5
+    scene = q.make_scene("refcornell", host.lib)
+    img, rad, sig, _ = _render(host, scene, w, h, spp, depth, seed=7)
+    ref = orc.render_nee(scene, w, h, spp, depth, seed=7, want_samples=True)
+    _check_parity(img, rad, sig, ref, w, h, spp)
+
+
+def test_soup_parity_subset(host, orc):
+    """A 100k-triangle soup (1% emitters), 8 bounces: full GPU frame, oracle on 1500 pixels."""
+    w, h = 320, 180
+    spp, depth = 4, 8
+    scene = q.make_scene("soup:n=100000,seed=1", host.lib)
+    img, rad, sig, _ = _render(host, scene, w, h, spp, depth, seed=3)
+    rng = np.random.default_rng(0)
+    pix = rng.choice(w * h, size=1500, replace=False).astype(np.uint32)
+    ref = orc.render_nee(scene, w, h, spp, depth, seed=3, pixels=pix, want_samples=True)
+    ys, xs = pix // w, pix % w
+    g_sig = sig[ys, xs]
+    g_rad = rad[ys, xs].astype(np.float64)
+    match = g_sig == ref["sig"]
+    assert match.mean() > 0.995, match.mean()
+    assert _rel(g_rad, ref["samples"]).max(-1)[match].max() <= REL_TOL
+    px_ok = match.all(-1)
+    p_err = _rel(img[ys, xs, :3].astype(np.float64), ref["mean"]).max(-1)
+    assert p_err[px_ok].max() <= REL_TOL
+
+
+def test_full_size_soup_parity_sampled_pixels(host, orc):
+    """The benchmark configuration (1M triangles, 1920x1080, depth 8) at 2 spp: the GPU frame
+    against the oracle on 300 random pixels, plus size-independent properties."""
+    w, h = 1920, 1080
+    spp, depth = 2, 8
+    scene = q.make_scene("soup:n=1000000,seed=0", host.lib)
+    img, rad, sig, st = _render(host, scene, w, h, spp, depth, seed=0)
+    assert np.isfinite(img).all() and (img[..., :3] >= 0).all()
+    assert np.all(img[..., 3] == 1.0)
+    rng = np.random.default_rng(1)
+    pix = rng.choice(w * h, size=300, replace=False).astype(np.uint32)
+    ref = orc.render_nee(scene, w, h, spp, depth, seed=0, pixels=pix, want_samples=True)
+    ys, xs = pix // w, pix % w
+    match = sig[ys, xs] == ref["sig"]
+    assert match.mean() > 0.99, match.mean()
+    assert _rel(rad[ys, xs].astype(np.float64), ref["samples"]).max(-1)[match].max() <= REL_TOL
+    # every path starts with exactly one camera ray; shadow rays never exceed vertices
+    assert st.camera_rays == w * h * spp
+    assert st.shadow_rays <= st.camera_rays + st.extension_rays
+
+
+def test_progressive_frames_equal_one_frame(host):
+    """Kahan accumulation over frames is order-preserving: 2 frames of 8 spp give the same
+    bits as one frame of 16 spp, and the wavefront size does not change results."""
+    scene = q.make_scene("cornell36", host.lib)
+    w = h = 64
+    host.set_scene(scene)
+    outs = []
+    for spp, frames, wave in ((16, 1, 0), (8, 2, 0), (16, 1, 1), (4, 4, 3)):
+        host.set_options(spp_per_frame=spp, max_depth=4, seed=5, wave_spp=wave, record_samples=0)
+        for f in range(frames):
+            host.render(w, h, dirty=(f == 0))
+        outs.append(host.readback())
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
+
+
+def test_deterministic_and_seed_sensitive(host):
+    scene = q.make_scene("soup:n=20000,seed=4", host.lib)
+    host.set_scene(scene)
+    host.set_options(spp_per_frame=4, max_depth=6, seed=1, record_samples=0, wave_spp=0)
+    host.render(160, 90, dirty=True)
+    a = host.readback()
+    host.render(160, 90, dirty=True)
+    b = host.readback()
+    assert np.array_equal(a, b)
+    host.set_options(spp_per_frame=4, max_depth=6, seed=2)
+    host.render(160, 90, dirty=True)
+    c = host.readback()
+    assert not np.array_equal(a, c)
+
+
+def test_aovs_match_oracle(host, orc):
+    w = h = 64
+    spp, depth = 4, 4
+    scene = q.make_scene("cornell36", host.lib)
+    host.set_scene(scene)
+    host.set_options(spp_per_frame=spp, max_depth=depth, seed=0, record_samples=1)
+    host.render(w, h, dirty=True)
+    aov = host.readback_aov()
+    _, sig = host.read_samples(spp)
+    ref = orc.render_nee(scene, w, h, spp, depth, seed=0, want_samples=True)
+    first_hit_ok = np.ones((h, w), bool)  # AOVs depend only on the camera ray's first hit
+    o = ref["aov"].reshape(h, w, 7)
+    assert np.abs(aov["albedo"][..., :3] - o[..., 0:3]).max() < 1e-5
+    assert np.abs(aov["depth"][..., 0] - o[..., 3]).max() < 1e-4
+    assert np.abs(aov["normal"][..., :3] - o[..., 4:7]).max() < 1e-4
+    assert np.all(aov["depth"][..., 3] == 1.0) and first_hit_ok.all()
+
+
+def test_white_furnace_closed_box(host):
+    """A closed box whose every triangle has albedo rho and emission Le: with emission on
+    camera hits plus NEE at each of D vertices, every pixel converges to Le * sum_{i<=D} rho^i."""
+    rho, le, depth = 0.5, 1.0, 4
+    s = q.make_scene("cornell36", host.lib)
+    box = np.array([[0, 0, 0, 1, 0, 0, 1, 0, 1], [0, 0, 0, 1, 0, 1, 0, 0, 1],   # floor
+                    [0, 1, 0, 1, 1, 1, 1, 1, 0], [0, 1, 0, 0, 1, 1, 1, 1, 1],   # ceiling
+                    [0, 0, 1, 1, 0, 1, 1, 1, 1], [0, 0, 1, 1, 1, 1, 0, 1, 1],   # back
+                    [0, 0, 0, 0, 1, 0, 1, 1, 0], [0, 0, 0, 1, 1, 0, 1, 0, 0],   # front
+                    [0, 0, 0, 0, 0, 1, 0, 1, 1], [0, 0, 0, 0, 1, 1, 0, 1, 0],   # x = 0
+                    [1, 0, 0, 1, 1, 0, 1, 1, 1], [1, 0, 0, 1, 1, 1, 1, 0, 1]],  # x = 1
+                   np.float32)
+    n = box.shape[0]
+    scene = q.Scene(box, np.full((n, 3), rho, np.float32), np.full((n, 3), le, np.float32),
+                    {"position": (0.5, 0.5, 0.5), "target": (0.5, 0.5, 1.0), "fov": 60.0})
+    del s
+    host.set_scene(scene)
+    host.set_options(spp_per_frame=64, max_depth=depth, seed=0, record_samples=0)
+    host.render(64, 64, dirty=True)
+    img = host.readback()[..., :3]
+    expect = le * sum(rho ** i for i in range(depth + 1))
+    assert abs(img.mean() / expect - 1.0) < 5e-3, (img.mean(), expect)
+
+
+def test_reference_integrator_matches_reference_shader(host, golden):
+    """The CUDA restatement of plugin.mm's path_trace (quads, brute force, the reference's
+    seeding and Russian roulette) against the shader run on the CPU, 24x24, 16 frames."""
+    r = golden["render"]
+    w, h, frames = r["width"], r["height"], r["frames"]
+    scene = q.make_scene("refcornell", host.lib)
+    host.set_scene(scene)
+    host.set_options(integrator=1, spp_per_frame=1, max_depth=5, record_samples=0)
+    for f in range(frames):
+        host.render(w, h, camera=r["camera"], dirty=(f == 0))
+    aov = host.readback_aov()
+    ref = np.array(r["beauty"], np.float64).reshape(h, w, 4)[..., :3]
+    err = _rel(aov["beauty"][..., :3].astype(np.float64), ref).max(-1)
+    assert (err <= REL_TOL).mean() >= 0.98, (np.sort(err.ravel())[-8:])
+    assert np.abs(aov["albedo"][..., :3] - np.array(r["albedo"]).reshape(h, w, 4)[..., :3]).max() < 1e-4
+    host.set_options(integrator=0, spp_per_frame=1, max_depth=4)
+
+
+def test_tonemap_into_device_buffer(host):
+    import torch
+
+    w = h = 32
+    host.set_scene(q.make_scene("cornell36", host.lib))
+    host.set_options(spp_per_frame=4, max_depth=4, seed=0, record_samples=0)
+    buf = torch.zeros(w * h * 4, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    host.render(w, h, dirty=True, drawable=buf.data_ptr())
+    hdr = host.readback()[..., :3]
+    host.synchronize()
+    ldr = buf.cpu().numpy().reshape(h, w, 4)
+    expect = np.clip(np.power(hdr / (hdr + 1.0), 1.0 / 2.2) * 255.0 + 0.5, 0, 255).astype(np.uint8)
+    assert np.abs(ldr[..., :3].astype(int) - expect.astype(int)).max() <= 1
+    assert np.all(ldr[..., 3] == 255)
