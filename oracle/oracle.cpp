@@ -418,12 +418,19 @@ template <class R> void nee_sample(const SceneR<R>& s, const CamBasis& cb, const
                 const R cos_x = dot(n, wi);
                 const V3<R> nl = cross(e1, e2);
                 const R area2 = std::sqrt(dot(nl, nl));
-                const R cos_l = std::fabs(dot(nl, wi)) / area2;
+                const R cl = dot(nl, wi);
+                const R cos_l = std::fabs(cl) / area2;
                 if (cos_x > R(0) && cos_l > R(0) && d2 > R(0)) {
                     nee = true;
                     cnt.shadow++;
+                    // Visibility from the light sample lifted by eps along the light normal
+                    // towards the shading side, to just short of the lifted shading point.
+                    const R side = cl < R(0) ? R(c.eps) : -R(c.eps);
+                    const V3<R> so = yl + nl * (side / area2);
+                    const V3<R> sd = org - so;
+                    const R sdist = std::sqrt(dot(sd, sd));
                     R ts, su2, sw2;
-                    const int occ = trace(s, org, wi, dist * (R(1) - R(1e-4)), -1, true, ts, su2, sw2);
+                    const int occ = trace(s, so, sd / sdist, sdist * (R(1) - R(1e-4)), -1, true, ts, su2, sw2);
                     if (occ < 0) {
                         const R g = cos_x * cos_l / d2 * (R(0.5) * area2) * R(ne) / R(3.14159265358979323846);
                         const V3<R> le = load3<R>(s.emission + 3ull * l);

@@ -1,20 +1,8 @@
-// wavefront.cu - the NEE path tracer as a wavefront of kernels, plus the Renderer host code.
-//
-// One wave = wave_spp samples of every pixel. Per wave:
-//   k_camera                 camera rays for every (sample, pixel) -> ray queue
-//   for bounce k = 1..D:
-//     k_trace_closest        persistent, warp-fetched closest-hit traversal of the queue
-//     k_shade                emission (k == 1), AOVs (k == 1), light sample -> shadow queue,
-//                            cosine-weighted continuation -> next ray queue; both queues are
-//                            compacted with one atomic per warp (ballot + popc)
-//     k_trace_shadow         persistent any-hit traversal; unoccluded rays add their
-//                            contribution to the owning path's radiance
-//   k_accumulate             per pixel, Kahan-adds the wave's samples in sample order
-// Paths are addressed by a stable id (sample-in-wave * slots + tile-ordered pixel slot); a
-// path has at most one ray in each queue, so no two threads ever update the same path.
-#include "common.cuh"
+// wavefront.cu - host side of the NEE path tracer: the Renderer (scene upload, per-frame
+// LBVH, the wavefront launch sequence, accumulation, readback, statistics). The device
+// kernels are in wavefront_kernels.cuh.
 #include "renderer.hpp"
-#include "trace.cuh"
+#include "wavefront_kernels.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -22,357 +10,13 @@
 
 namespace quasi {
 
-// ---------------------------------------------------------------------------- kernels
-
-struct FrameParams {
-    CameraBasis cam;
-    uint32_t width, height, tiles_x, slots;
-    uint32_t wave_spp, sample_base;
-    uint32_t seed, max_depth;
-    float eps;
-    uint32_t frame_spp, wave_offset;
-};
-
-struct SceneDev {
-    const float4* tri_in;   // original order, v0 v1 v2
-    const float4* albedo;
-    const float4* emission;
-    const int* emitters;
-    const float4* nodes;
-    const float4* tris;     // leaf order, v0+orig, e1, e2
-    uint32_t n_tris, n_emit;
-};
-
-struct PathDev {
-    float4* beta;
-    float4* lpath;
-    float4* aov_a;   // first-hit albedo (rgb) + depth (w)
-    float4* aov_n;   // first-hit remapped normal
-    uint32_t* sig;   // path signatures (record mode) or null
-};
-
-// Pixel slots are ordered in 8x4 tiles so a warp's camera rays cover a compact patch.
-__device__ __forceinline__ void slot_to_xy(uint32_t slot, uint32_t tiles_x, uint32_t& x, uint32_t& y) {
-    const uint32_t tile = slot >> 5, in = slot & 31u;
-    const uint32_t ty = tile / tiles_x, tx = tile - ty * tiles_x;
-    x = tx * 8u + (in & 7u);
-    y = ty * 4u + (in >> 3);
-}
-__device__ __forceinline__ uint32_t xy_to_slot(uint32_t x, uint32_t y, uint32_t tiles_x) {
-    return ((((y >> 2) * tiles_x) + (x >> 3)) << 5) | ((y & 3u) << 3) | (x & 7u);
-}
-
-__device__ __forceinline__ void kahan_add(float& sum, float& comp, float x) {
-    const float y = x - comp;
-    const float t = sum + y;
-    comp = (t - sum) - y;
-    sum = t;
-}
-
-__global__ void __launch_bounds__(256) k_pack_tris(const float* __restrict__ raw, uint32_t n, float4* __restrict__ out) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float* v = raw + 9ull * i;
-    out[3 * i + 0] = make_float4(v[0], v[1], v[2], 0.f);
-    out[3 * i + 1] = make_float4(v[3], v[4], v[5], 0.f);
-    out[3 * i + 2] = make_float4(v[6], v[7], v[8], 0.f);
-}
-
-__global__ void __launch_bounds__(256) k_camera(FrameParams f, PathDev p, float4* __restrict__ q, int* __restrict__ q_count) {
-    const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= f.wave_spp * f.slots) return;  // slots is a multiple of 32: whole warps leave
-    const uint32_t j = gid / f.slots, slot = gid - j * f.slots;
-    uint32_t x, y;
-    slot_to_xy(slot, f.tiles_x, x, y);
-    const bool valid = x < f.width && y < f.height;
-    float3 d = mk3(0.f, 0.f, 0.f);
-    if (valid) {
-        const uint32_t pixel = y * f.width + x;
-        uint32_t st = path_key(f.seed, pixel, f.sample_base + j, 0u);
-        const float jx = rng_next(st);
-        const float jy = rng_next(st);
-        const float u = (static_cast<float>(x) + jx) / static_cast<float>(f.width);
-        const float v = 1.0f - (static_cast<float>(y) + jy) / static_cast<float>(f.height);
-        d = camera_dir(f.cam, u, v);
-        p.beta[gid] = make_float4(1.f, 1.f, 1.f, 0.f);
-        p.lpath[gid] = make_float4(0.f, 0.f, 0.f, 0.f);
-        p.aov_a[gid] = make_float4(0.f, 0.f, 0.f, 0.f);
-        p.aov_n[gid] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (p.sig) p.sig[gid] = 0u;
-    }
-    const int pos = warp_append(0xffffffffu, valid, q_count);
-    if (valid) {
-        q[2 * pos] = make_float4(f.cam.origin.x, f.cam.origin.y, f.cam.origin.z, __int_as_float(static_cast<int>(gid)));
-        q[2 * pos + 1] = make_float4(d.x, d.y, d.z, __int_as_float(-1));
-    }
-}
-
-template <bool STATS>
-__device__ __forceinline__ void flush_counters(const TraceCounters& c, unsigned long long* stats) {
-    if (!STATS) return;
-    uint32_t a = c.nodes, b = c.tris;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        a += __shfl_xor_sync(0xffffffffu, a, o);
-        b += __shfl_xor_sync(0xffffffffu, b, o);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(&stats[0], static_cast<unsigned long long>(a));
-        atomicAdd(&stats[1], static_cast<unsigned long long>(b));
-    }
-}
-
-// Persistent closest-hit traversal: warps grab 32 rays at a time from the queue.
-template <bool STATS>
-__global__ void __launch_bounds__(256) k_trace_closest(SceneDev s, const float4* __restrict__ q,
-                                                       float4* __restrict__ hits, const int* __restrict__ count,
-                                                       int capacity, int* __restrict__ fetch,
-                                                       uint32_t* __restrict__ err, unsigned long long* __restrict__ stats) {
-    const int n = min(*count, capacity);
-    const int lane = threadIdx.x & 31;
-    uint32_t e = 0;
-    TraceCounters c;
-    while (true) {
-        int base = 0;
-        if (lane == 0) base = atomicAdd(fetch, 32);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n) break;
-        const int i = base + lane;
-        if (i < n) {
-            const float4 r0 = q[2 * i], r1 = q[2 * i + 1];
-            const RayInv r = make_ray(xyz(r0), xyz(r1));
-            float t, bu, bv;
-            const int prim = trace_bvh<false, STATS>(s.nodes, s.tris, s.n_tris, r, __int_as_float(0x7f800000),
-                                                     __float_as_int(r1.w), t, bu, bv, e, c);
-            hits[i] = make_float4(t, __int_as_float(prim), bu, bv);
-        }
-    }
-    if (e) atomicOr(err, e);
-    flush_counters<STATS>(c, stats);
-}
-
-template <bool STATS>
-__global__ void __launch_bounds__(256) k_trace_shadow(SceneDev s, PathDev p, const float4* __restrict__ sq,
-                                                      const int* __restrict__ count, int capacity,
-                                                      int* __restrict__ fetch, uint32_t* __restrict__ err,
-                                                      unsigned long long* __restrict__ stats) {
-    const int n = min(*count, capacity);
-    const int lane = threadIdx.x & 31;
-    uint32_t e = 0;
-    TraceCounters c;
-    while (true) {
-        int base = 0;
-        if (lane == 0) base = atomicAdd(fetch, 32);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n) break;
-        const int i = base + lane;
-        if (i < n) {
-            const float4 r0 = sq[3 * i], r1 = sq[3 * i + 1], r2 = sq[3 * i + 2];
-            const RayInv r = make_ray(xyz(r0), xyz(r1));
-            float t, bu, bv;
-            const int hit = trace_bvh<true, STATS>(s.nodes, s.tris, s.n_tris, r, r1.w, -1, t, bu, bv, e, c);
-            const int pid = __float_as_int(r0.w);
-            if (hit < 0) {
-                float4 L = p.lpath[pid];
-                L.x += r2.x;
-                L.y += r2.y;
-                L.z += r2.z;
-                p.lpath[pid] = L;
-            }
-            if (p.sig) p.sig[pid] = sig_mix(p.sig[pid], hit < 0 ? k_sig_lit : k_sig_shadowed);
-        }
-    }
-    if (e) atomicOr(err, e);
-    flush_counters<STATS>(c, stats + 2);
-}
-
-// Adds the frame's queue lengths (rays traced) to the cumulative counter stats[4]; one
-// warp, so the timed loop needs no host synchronisation to know how many rays it traced.
-__global__ void k_tally(const int* __restrict__ counters, uint32_t waves, uint32_t depth,
-                        unsigned long long* __restrict__ stats) {
-    unsigned long long sum = 0;
-    for (uint32_t i = threadIdx.x; i < waves * 2 * depth; i += 32) {
-        const uint32_t w = i / (2 * depth), k = i - w * 2 * depth;
-        sum += static_cast<unsigned long long>(max(counters[w * 4 * depth + k], 0));
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-    if (threadIdx.x == 0) stats[4] += sum;
-}
-
-__global__ void __launch_bounds__(256) k_shade(FrameParams f, SceneDev s, PathDev p, uint32_t bounce,
-                                               const float4* __restrict__ q, const float4* __restrict__ hits,
-                                               const int* __restrict__ count, int capacity, float4* __restrict__ next_q,
-                                               int* __restrict__ next_count, float4* __restrict__ shadow_q,
-                                               int* __restrict__ shadow_count) {
-    const int n = min(*count, capacity);
-    const int lane = threadIdx.x & 31;
-    const int stride = gridDim.x * blockDim.x;
-    for (int base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; base < n; base += stride) {
-        const int i = base + lane;
-        bool want_shadow = false, want_next = false;
-        float3 org = mk3(0.f, 0.f, 0.f), wi = org, contrib = org, nd = org;
-        float tmax_s = 0.f;
-        int pid = 0, prim = -1;
-        if (i < n) {
-            const float4 r0 = q[2 * i], r1 = q[2 * i + 1];
-            const float4 h = hits[i];
-            pid = __float_as_int(r0.w);
-            prim = __float_as_int(h.y);
-            if (prim < 0) {
-                if (p.sig) p.sig[pid] = sig_mix(p.sig[pid], k_sig_miss);
-            } else {
-                const float3 d = xyz(r1);
-                const float3 a = xyz(__ldg(&s.tri_in[3 * prim]));
-                const float3 e1 = xyz(__ldg(&s.tri_in[3 * prim + 1])) - a;
-                const float3 e2 = xyz(__ldg(&s.tri_in[3 * prim + 2])) - a;
-                const float3 x = a + e1 * h.z + e2 * h.w;  // barycentric hit point, on the plane
-                float3 nrm = normalize(cross(e1, e2));
-                if (dot(nrm, d) > 0.0f) nrm = -nrm;
-                const float3 alb = xyz(__ldg(&s.albedo[prim]));
-                float3 beta = xyz(p.beta[pid]);
-                uint32_t sig = p.sig ? sig_mix(p.sig[pid], static_cast<uint32_t>(prim)) : 0u;
-                if (bounce == 1) {
-                    const float3 em = xyz(__ldg(&s.emission[prim]));
-                    p.lpath[pid] = make_float4(em.x, em.y, em.z, 0.f);
-                    const float3 aa = max3(em) > 0.1f ? em : alb;
-                    const float depth = fminf(fmaxf((h.x - 1.0f) * 0.25f, 0.0f), 1.0f);
-                    p.aov_a[pid] = make_float4(aa.x, aa.y, aa.z, depth);
-                    p.aov_n[pid] = make_float4(nrm.x * 0.5f + 0.5f, nrm.y * 0.5f + 0.5f, nrm.z * 0.5f + 0.5f, 0.f);
-                }
-                const uint32_t j = static_cast<uint32_t>(pid) / f.slots;
-                uint32_t px, py;
-                slot_to_xy(static_cast<uint32_t>(pid) - j * f.slots, f.tiles_x, px, py);
-                uint32_t st = path_key(f.seed, py * f.width + px, f.sample_base + j, bounce);
-                const uint32_t sel = pcg_hash(st);
-                st = sel;
-                const float r1 = rng_next(st);
-                const float r2 = rng_next(st);
-                org = x + nrm * f.eps;
-                if (s.n_emit > 0) {
-                    const int l = __ldg(&s.emitters[static_cast<uint32_t>((static_cast<uint64_t>(sel) * s.n_emit) >> 32)]);
-                    if (l != prim) {
-                        const float3 la = xyz(__ldg(&s.tri_in[3 * l]));
-                        const float3 e1 = xyz(__ldg(&s.tri_in[3 * l + 1])) - la;
-                        const float3 e2 = xyz(__ldg(&s.tri_in[3 * l + 2])) - la;
-                        const float su = sqrtf(r1);
-                        const float3 yl = la + e1 * (su * (1.0f - r2)) + e2 * (su * r2);
-                        // (y - x) first: both lie on their planes, so a small surface-to-light gap
-                        // keeps its digits; subtracting the rounded offset origin would not.
-                        const float3 dv = (yl - x) - nrm * f.eps;
-                        const float d2 = dot(dv, dv);
-                        const float dist = sqrtf(d2);
-                        wi = dv * (1.0f / dist);
-                        const float cos_x = dot(nrm, wi);
-                        const float3 nl = cross(e1, e2);
-                        const float area2 = sqrtf(dot(nl, nl));
-                        const float cos_l = fabsf(dot(nl, wi)) / area2;
-                        if (cos_x > 0.0f && cos_l > 0.0f && d2 > 0.0f) {
-                            const float g = cos_x * cos_l / d2 * (0.5f * area2) * static_cast<float>(s.n_emit) * k_inv_pi;
-                            contrib = beta * alb * xyz(__ldg(&s.emission[l])) * g;
-                            tmax_s = dist * (1.0f - 1e-4f);
-                            want_shadow = true;
-                        }
-                    }
-                }
-                if (!want_shadow) sig = sig_mix(sig, k_sig_no_nee);
-                const float r3 = rng_next(st);
-                const float r4 = rng_next(st);
-                nd = cosine_sample(nrm, r3, r4);
-                beta = beta * alb;
-                p.beta[pid] = make_float4(beta.x, beta.y, beta.z, 0.f);
-                if (p.sig) p.sig[pid] = sig;
-                want_next = bounce < f.max_depth && max3(beta) > 0.0f;
-            }
-        }
-        const int ps = warp_append(0xffffffffu, want_shadow, shadow_count);
-        if (want_shadow) {
-            shadow_q[3 * ps] = make_float4(org.x, org.y, org.z, __int_as_float(pid));
-            shadow_q[3 * ps + 1] = make_float4(wi.x, wi.y, wi.z, tmax_s);
-            shadow_q[3 * ps + 2] = make_float4(contrib.x, contrib.y, contrib.z, 0.f);
-        }
-        const int pn = warp_append(0xffffffffu, want_next, next_count);
-        if (want_next) {
-            next_q[2 * pn] = make_float4(org.x, org.y, org.z, __int_as_float(pid));
-            next_q[2 * pn + 1] = make_float4(nd.x, nd.y, nd.z, __int_as_float(prim));
-        }
-    }
-}
-
-__global__ void __launch_bounds__(256) k_accumulate(FrameParams f, PathDev p, float4* __restrict__ accum,
-                                                    float4* __restrict__ comp, float4* __restrict__ aov_a,
-                                                    float4* __restrict__ aov_n, float* __restrict__ rec_rad,
-                                                    uint32_t* __restrict__ rec_sig) {
-    const uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pixel >= f.width * f.height) return;
-    const uint32_t y = pixel / f.width, x = pixel - y * f.width;
-    const uint32_t slot = xy_to_slot(x, y, f.tiles_x);
-    float4 sum = accum[pixel], c = comp[pixel], A = aov_a[pixel], N = aov_n[pixel];
-    for (uint32_t j = 0; j < f.wave_spp; ++j) {
-        const uint32_t pid = j * f.slots + slot;
-        const float4 L = p.lpath[pid];
-        kahan_add(sum.x, c.x, L.x);
-        kahan_add(sum.y, c.y, L.y);
-        kahan_add(sum.z, c.z, L.z);
-        const float4 a = p.aov_a[pid], nn = p.aov_n[pid];
-        A.x += a.x; A.y += a.y; A.z += a.z; A.w += a.w;
-        N.x += nn.x; N.y += nn.y; N.z += nn.z;
-        if (rec_rad) {
-            const size_t idx = static_cast<size_t>(pixel) * f.frame_spp + f.wave_offset + j;
-            rec_rad[3 * idx] = L.x;
-            rec_rad[3 * idx + 1] = L.y;
-            rec_rad[3 * idx + 2] = L.z;
-            rec_sig[idx] = p.sig ? p.sig[pid] : 0u;
-        }
-    }
-    accum[pixel] = sum;
-    comp[pixel] = c;
-    aov_a[pixel] = A;
-    aov_n[pixel] = N;
-}
-
-// Mean image (RGBA, alpha 1) from the accumulation: mode 0 beauty, 1 albedo, 2 normal, 3 depth.
-__global__ void __launch_bounds__(256) k_resolve(const float4* __restrict__ accum, const float4* __restrict__ aov_a,
-                                                 const float4* __restrict__ aov_n, uint32_t n_px, float count,
-                                                 int mode, float4* __restrict__ out) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_px) return;
-    float4 v;
-    if (mode == 0) v = accum[i];
-    else if (mode == 1 || mode == 3) v = aov_a[i];
-    else v = aov_n[i];
-    float4 o;
-    if (count <= 0.0f) o = make_float4(0.f, 0.f, 0.f, 1.f);
-    else if (mode == 3) { const float d = v.w / count; o = make_float4(d, d, d, 1.f); }
-    else o = make_float4(v.x / count, v.y / count, v.z / count, 1.f);
-    out[i] = o;
-}
-
-// plugin.mm:334-350: Reinhard then gamma 1/2.2, written as RGBA8 into a device buffer.
-__global__ void __launch_bounds__(256) k_tonemap(const float4* __restrict__ accum, uint32_t n_px, float count,
-                                                 uchar4* __restrict__ out) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_px) return;
-    const float4 s = accum[i];
-    const float inv = count > 0.f ? 1.0f / count : 0.f;
-    float c[3] = {s.x * inv, s.y * inv, s.z * inv};
-    unsigned char b[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const float m = c[k] / (c[k] + 1.0f);
-        const float g = powf(fmaxf(m, 0.0f), 1.0f / 2.2f);
-        b[k] = static_cast<unsigned char>(fminf(g * 255.0f + 0.5f, 255.0f));
-    }
-    out[i] = make_uchar4(b[0], b[1], b[2], 255);
-}
-
 // ---------------------------------------------------------------------------- host
 
 namespace {
 
 inline uint32_t ceil_div(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
 
-CameraBasis make_camera_basis(const Q_camera& c, uint32_t w, uint32_t h) {
+CameraFF make_camera_basis(const Q_camera& c, uint32_t w, uint32_t h) {
     // plugin.mm:649-674 (host direction) and plugin.mm:134-147 (shader basis), in double.
     double dir[3] = {double(c.target[0]) - c.position[0], double(c.target[1]) - c.position[1],
                      double(c.target[2]) - c.position[2]};
@@ -389,7 +33,7 @@ CameraBasis make_camera_basis(const Q_camera& c, uint32_t w, uint32_t h) {
     const double theta = double(c.fov) * 3.14159265358979323846 / 180.0;
     const double vh = 2.0 * std::tan(theta / 2.0);
     const double vw = (double(w) / double(h)) * vh;
-    CameraBasis b;
+    CameraFF b;
     b.origin = make_float3(c.position[0], c.position[1], c.position[2]);
     double H[3], V[3], LL[3];
     for (int k = 0; k < 3; ++k) {
@@ -397,9 +41,14 @@ CameraBasis make_camera_basis(const Q_camera& c, uint32_t w, uint32_t h) {
         V[k] = vh * u2[k];
         LL[k] = double(c.position[k]) - H[k] * 0.5 - V[k] * 0.5 - wv[k];
     }
-    b.horizontal = make_float3(float(H[0]), float(H[1]), float(H[2]));
-    b.vertical = make_float3(float(V[0]), float(V[1]), float(V[2]));
-    b.lower_left = make_float3(float(LL[0]), float(LL[1]), float(LL[2]));
+    // Each double splits into hi = nearest float and lo = nearest float of the remainder.
+    auto split = [](const double* d, float3& hi, float3& lo) {
+        hi = make_float3(float(d[0]), float(d[1]), float(d[2]));
+        lo = make_float3(float(d[0] - double(hi.x)), float(d[1] - double(hi.y)), float(d[2] - double(hi.z)));
+    };
+    split(H, b.h_hi, b.h_lo);
+    split(V, b.v_hi, b.v_lo);
+    split(LL, b.ll_hi, b.ll_lo);
     return b;
 }
 
@@ -423,7 +72,7 @@ Renderer::~Renderer() {
     bvh_.release();
     for (DeviceBuffer* b : {&raw_vertices_, &tri_in_, &albedo_, &emission_, &emitters_, &quads_, &accum_, &comp_,
                             &aov_albedo_, &aov_normal_, &record_rad_, &record_sig_, &queue_[0], &queue_[1], &hits_,
-                            &shadow_, &beta_, &lpath_, &aov_a_, &aov_n_, &sig_, &counters_, &stats_dev_, &err_dev_})
+                            &shadow_, &beta_, &lpath_, &aov_a_, &aov_n_, &sig_, &ray_ff_, &counters_, &stats_dev_, &err_dev_})
         b->release();
     if (counters_host_) cudaFreeHost(counters_host_);
     if (stats_host_) cudaFreeHost(stats_host_);
@@ -598,6 +247,7 @@ int Renderer::ensure_wave_buffers(uint32_t paths) {
     R_TRY(aov_a_.reserve(sizeof(float4) * paths), "aov");
     R_TRY(aov_n_.reserve(sizeof(float4) * paths), "aov");
     R_TRY(sig_.reserve(sizeof(uint32_t) * paths), "sig");
+    R_TRY(ray_ff_.reserve(sizeof(float4) * 3ull * paths), "ray_ff");
     wave_capacity_ = paths;
     return QUASI_OK;
 }
@@ -682,8 +332,8 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
     const LbvhView bv = bvh_.view();
     SceneDev sd{tri_in_.as<float4>(), albedo_.as<float4>(), emission_.as<float4>(), emitters_.as<int>(),
                 bv.nodes, bv.tris, n_tris_, n_emit_};
-    PathDev pd{beta_.as<float4>(), lpath_.as<float4>(), aov_a_.as<float4>(), aov_n_.as<float4>(),
-               opt_.record_samples ? sig_.as<uint32_t>() : nullptr};
+    PathDev pd{beta_.as<float4>(),  lpath_.as<float4>(), aov_a_.as<float4>(),
+               aov_n_.as<float4>(), ray_ff_.as<float4>(), opt_.record_samples ? sig_.as<uint32_t>() : nullptr};
     FrameParams f{};
     f.cam = make_camera_basis(camera_, width_, height_);
     f.width = width_;

@@ -1,0 +1,48 @@
+// Host build of quasi_gb300/csrc/ffmath.cuh: the device intrinsics it uses are IEEE
+// round-to-nearest float operations, so mapping them to host float arithmetic (compiled with
+// -ffp-contract=off) reproduces the device results. Prints the worst relative error of each
+// double-float operation against long double over random inputs.
+#include <cmath>
+#include <cstdio>
+#include <random>
+
+#include <cuda_runtime.h>
+
+inline float __fadd_rn(float a, float b) { return a + b; }
+inline float __fsub_rn(float a, float b) { return a - b; }
+inline float __fmul_rn(float a, float b) { return a * b; }
+inline float __fdiv_rn(float a, float b) { return a / b; }
+inline float __fsqrt_rn(float a) { return std::sqrt(a); }
+inline float __fmaf_rn(float a, float b, float c) { return std::fma(a, b, c); }
+#include "../quasi_gb300/csrc/ffmath.cuh"
+
+using quasi::ff;
+static long double val(ff a) { return (long double)a.hi + (long double)a.lo; }
+
+int main() {
+    std::mt19937_64 rng(7);
+    std::uniform_real_distribution<double> U(-2.0, 2.0), P(1e-3, 4.0), R01(0.0, 1.0);
+    long double e_add = 0, e_mul = 0, e_div = 0, e_sqrt = 0, e_sin = 0, e_cos = 0;
+    auto mk = [&](double d) { ff x; x.hi = (float)d; x.lo = (float)(d - (double)x.hi); return x; };
+    for (int i = 0; i < 200000; ++i) {
+        const ff a = mk(U(rng)), b = mk(U(rng)), p = mk(P(rng));
+        const long double A = val(a), B = val(b), Pv = val(p);
+        auto rel = [](long double got, long double want) {
+            return fabsl(got - want) / fmaxl(fabsl(want), 1e-30L);
+        };
+        const long double scale = fmaxl(fabsl(A), fabsl(B));
+        e_add = fmaxl(e_add, fabsl(val(quasi::ff_add(a, b)) - (A + B)) / fmaxl(scale, 1e-30L));
+        e_mul = fmaxl(e_mul, rel(val(quasi::ff_mul(a, b)), A * B));
+        e_div = fmaxl(e_div, rel(val(quasi::ff_div(a, p)), A / Pv));
+        e_sqrt = fmaxl(e_sqrt, rel(val(quasi::ff_sqrt(p)), sqrtl(Pv)));
+        const float x = (float)(2.0 * R01(rng));
+        ff s, c;
+        quasi::ff_sincospi(x, s, c);
+        const long double pi = 3.141592653589793238462643383279502884L;
+        e_sin = fmaxl(e_sin, fabsl(val(s) - sinl(pi * (long double)x)));
+        e_cos = fmaxl(e_cos, fabsl(val(c) - cosl(pi * (long double)x)));
+    }
+    std::printf("add %.3Le\nmul %.3Le\ndiv %.3Le\nsqrt %.3Le\nsin %.3Le\ncos %.3Le\n", e_add, e_mul, e_div, e_sqrt,
+                e_sin, e_cos);
+    return 0;
+}

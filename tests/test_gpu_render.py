@@ -2,8 +2,10 @@
 
 Tolerance: per-pixel relative error |gpu - oracle| / max(|oracle|, 1e-3) <= 1e-4 for every
 pixel whose path signatures (the sequence of triangles hit and shadow-ray outcomes) all
-agree with the oracle's. A path whose FP32 branch decision differs from FP64 (a ray grazing
-an edge) is counted as divergent; divergent pixels must stay rare.
+agree with the oracle's, and the same bound per sample. A path whose FP32 traversal decision
+differs from FP64 (a ray within ~1e-7 of a triangle edge) is counted as divergent; at most
+2 pixels in 10,000 may contain one (measured: 2 divergent samples of 1,048,576 on the
+256x256x16 Cornell box).
 """
 from __future__ import annotations
 
@@ -41,7 +43,7 @@ def _rel(a, b):
     return np.abs(a - b) / np.maximum(np.abs(b), FLOOR)
 
 
-def _check_parity(img, rad, sig, ref, w, h, spp, max_divergent=1e-3):
+def _check_parity(img, rad, sig, ref, w, h, spp, max_divergent=2e-4):
     osig = ref["sig"].reshape(h, w, spp)
     osamp = ref["samples"].reshape(h, w, spp, 3)
     match = sig == osig
@@ -93,7 +95,7 @@ def test_soup_parity_subset(host, orc):
     g_sig = sig[ys, xs]
     g_rad = rad[ys, xs].astype(np.float64)
     match = g_sig == ref["sig"]
-    assert match.mean() > 0.995, match.mean()
+    assert match.mean() >= 0.999, match.mean()
     assert _rel(g_rad, ref["samples"]).max(-1)[match].max() <= REL_TOL
     px_ok = match.all(-1)
     p_err = _rel(img[ys, xs, :3].astype(np.float64), ref["mean"]).max(-1)
@@ -114,7 +116,7 @@ def test_full_size_soup_parity_sampled_pixels(host, orc):
     ref = orc.render_nee(scene, w, h, spp, depth, seed=0, pixels=pix, want_samples=True)
     ys, xs = pix // w, pix % w
     match = sig[ys, xs] == ref["sig"]
-    assert match.mean() > 0.99, match.mean()
+    assert match.mean() >= 0.999, match.mean()
     assert _rel(rad[ys, xs].astype(np.float64), ref["samples"]).max(-1)[match].max() <= REL_TOL
     # every path starts with exactly one camera ray; shadow rays never exceed vertices
     assert st.camera_rays == w * h * spp
