@@ -228,21 +228,23 @@ def run_ours(args) -> None:
     value = rays / (total_ms / 1e3) / 1e6
 
     # end to end through the plugin ABI: pinned host scene upload + render + host readback
-    vert_pinned = torch.from_numpy(np.ascontiguousarray(scene.vertices)).pin_memory()
-    e2e_steps = max(2, min(args.steps, 3))
-    torch.cuda.synchronize()
-    r0 = host.stats().total_rays
-    t0 = time.perf_counter()
-    for i in range(e2e_steps):
-        host.set_options(seed=50_000 + i, **opts)
-        host.update_vertices(vert_pinned.data_ptr(), scene.tri_count)
-        host.render(WIDTH, HEIGHT, dirty=True, stream=stream.cuda_stream)
-        img = host.readback()
-    e2e_s = time.perf_counter() - t0
-    e2e_rays = host.stats().total_rays - r0
-    e2e = {"value": e2e_rays / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": int(scene.vertices.nbytes),
-           "d2h_bytes_per_step": int(img.nbytes), "steps": e2e_steps,
-           "path": "Q_cuda_update_vertices(pinned host) + Q_plugin_render + Q_plugin_readback"}
+    e2e = None
+    if not args.no_e2e:
+        vert_pinned = torch.from_numpy(np.ascontiguousarray(scene.vertices)).pin_memory()
+        e2e_steps = max(2, min(args.steps, 3))
+        torch.cuda.synchronize()
+        r0 = host.stats().total_rays
+        t0 = time.perf_counter()
+        for i in range(e2e_steps):
+            host.set_options(seed=50_000 + i, **opts)
+            host.update_vertices(vert_pinned.data_ptr(), scene.tri_count)
+            host.render(WIDTH, HEIGHT, dirty=True, stream=stream.cuda_stream)
+            img = host.readback()
+        e2e_s = time.perf_counter() - t0
+        e2e_rays = host.stats().total_rays - r0
+        e2e = {"value": e2e_rays / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": int(scene.vertices.nbytes),
+               "d2h_bytes_per_step": int(img.nbytes), "steps": e2e_steps,
+               "path": "Q_cuda_update_vertices(pinned host) + Q_plugin_render + Q_plugin_readback"}
 
     # roofline of the dominant kernel
     peak, peak_kind = _peaks()
@@ -298,7 +300,15 @@ def main() -> None:
     ap.add_argument("--trace-block", type=int, default=0)
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    # Size overrides, for profiling captures on a small case only (not benchmark numbers).
+    ap.add_argument("--width", type=int, default=WIDTH)
+    ap.add_argument("--height", type=int, default=HEIGHT)
+    ap.add_argument("--spp", type=int, default=SPP)
     args = ap.parse_args()
+    globals().update(WIDTH=args.width, HEIGHT=args.height, SPP=args.spp)
+    if (args.width, args.height, args.spp) != (1920, 1080, 64):
+        globals()["WORKLOAD"] = f"soup-1M {args.width}x{args.height} {args.spp}spp depth8 (profiling case)"
     if args.impl == "reference":
         run_reference(args)
     else:
