@@ -274,6 +274,24 @@ Q_CUDA_EXPORT int Q_cuda_resolve_device(Q_plugin_handle* handle, float* device_r
 Q_CUDA_EXPORT int Q_cuda_radix_sort_pairs(uint32_t* device_keys, uint32_t* device_values,
                                           uint32_t n, uint32_t key_bits, void* stream);
 
+/* The same sort for callers that cannot let the library allocate device memory: a real-time
+ * frame loop where cudaMalloc/cudaFree could synchronise the device mid-frame, or a host that
+ * owns all device memory through its own pool. It has no counterpart in the reference.
+ * Scratch comes from one fixed array in device memory that every GPU loading the library
+ * holds until exit (QUASI_NOALLOC_SORT_SCRATCH_BYTES); the caller still owns keys and values.
+ * Limits and behaviour:
+ *  - n above QUASI_NOALLOC_SORT_MAX_KEYS returns QUASI_ERR_TOO_LARGE and touches nothing;
+ *  - the first call on a device looks up the array's device address (cudaGetSymbolAddress,
+ *    with that device current); make that first call before any stream capture;
+ *  - all calls share the one array and it keeps the last call's contents, so calls that
+ *    overlap on the GPU (other streams, other threads) race; serialise them on one stream;
+ *  - the sort is enqueued on `stream` and the function returns without waiting for it. */
+#define QUASI_ERR_TOO_LARGE -7 /* input larger than a fixed-capacity entry point accepts */
+#define QUASI_NOALLOC_SORT_MAX_KEYS 1048576u
+#define QUASI_NOALLOC_SORT_SCRATCH_BYTES 8912896u /* 2 x 4 MiB key/value buffers + 512 KiB histograms */
+Q_CUDA_EXPORT int Q_cuda_radix_sort_pairs_noalloc(uint32_t* device_keys, uint32_t* device_values,
+                                                  uint32_t n, uint32_t key_bits, void* stream);
+
 /* Runs the autotuner on the current scene/options and stores the result in the options
  * (wave_spp, trace_block). budget_ms bounds the time spent. */
 Q_CUDA_EXPORT int Q_cuda_autotune(Q_plugin_handle* handle, double budget_ms);

@@ -140,5 +140,6 @@ CUDA_SYMBOLS = {
     "Q_cuda_read_samples": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "Q_cuda_resolve_device": (C.c_int, [C.c_void_p, C.c_void_p]),
     "Q_cuda_radix_sort_pairs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]),
+    "Q_cuda_radix_sort_pairs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]),
     "Q_cuda_autotune": (C.c_int, [C.c_void_p, C.c_double]),
 }
