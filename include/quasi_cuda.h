@@ -192,8 +192,12 @@ typedef struct Q_cuda_options {
     uint32_t collect_stats;      /* count BVH node visits and triangle tests */
     uint32_t profile;            /* time every kernel launch with CUDA events */
     uint32_t megakernel;         /* 1 = one-kernel path tracer instead of the wavefront */
-    uint32_t smem_levels;        /* BVH levels staged in shared memory (0 = default) */
+    uint32_t smem_levels;        /* top BVH levels staged in shared memory per block
+                                    (0 = default 7, 1..9, 32 = none) */
     float ray_eps;               /* ray origin offset along the normal (1e-4) */
+    uint32_t refill_lanes;       /* trace kernels refill a warp once this many lanes idle
+                                    (1..32; 32 = refill only whole warps; 0 = default) */
+    uint32_t trace_steps;        /* node visits per lane between refill checks (0 = default) */
 } Q_cuda_options;
 
 /* Counters of the last frame (rays actually traced) and of the whole accumulation. */
@@ -291,6 +295,26 @@ Q_CUDA_EXPORT int Q_cuda_radix_sort_pairs(uint32_t* device_keys, uint32_t* devic
 #define QUASI_NOALLOC_SORT_SCRATCH_BYTES 8912896u /* 2 x 4 MiB key/value buffers + 512 KiB histograms */
 Q_CUDA_EXPORT int Q_cuda_radix_sort_pairs_noalloc(uint32_t* device_keys, uint32_t* device_values,
                                                   uint32_t n, uint32_t key_bits, void* stream);
+
+/* Replaces per-triangle materials from DEVICE arrays (tri_count*3 floats each; either may be
+ * NULL to keep it) and resets accumulation. The set of emitters (triangles whose emission
+ * was > 0 when the scene or host materials were last set) is kept. Used by optimisation
+ * loops that update materials on the GPU every step. */
+Q_CUDA_EXPORT int Q_cuda_set_materials_device(Q_plugin_handle* handle, const float* device_albedo,
+                                              const float* device_emission, uint32_t tri_count);
+
+/* Path-replay adjoint (no reference counterpart): for the current scene, camera, frame size
+ * and options (NEE integrator, max_depth <= 16), replays samples [sample_base,
+ * sample_base + spp) of every pixel from their RNG keys and writes
+ *   device_grad_albedo[3*i+c]   = dLoss/d albedo_i,c
+ *   device_grad_emission[3*i+c] = dLoss/d emission_i,c
+ * where Loss depends on the image I = mean of those samples through
+ * device_grad_image[3*(y*width+x)+c] = dLoss/dI(x,y,c) (top row first). All pointers are
+ * device pointers; the call is asynchronous on `stream` (a cudaStream_t; NULL = the plugin's
+ * stream; pass cudaStreamLegacy, (void*)1, for the legacy default stream). */
+Q_CUDA_EXPORT int Q_cuda_backward(Q_plugin_handle* handle, const float* device_grad_image, uint32_t spp,
+                                  uint32_t sample_base, float* device_grad_albedo,
+                                  float* device_grad_emission, void* stream);
 
 /* Runs the autotuner on the current scene/options and stores the result in the options
  * (wave_spp, trace_block). budget_ms bounds the time spent. */

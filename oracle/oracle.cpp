@@ -351,9 +351,19 @@ struct NeeConfig {
     float eps;
 };
 
-// One path sample of the NEE integrator (the conventions the CUDA kernels implement).
+// One vertex of a path as the adjoint needs it: the triangle hit, the NEE light (or -1) and
+// the NEE factor g times visibility.
+template <class R> struct PathVtx {
+    int prim;
+    int light;
+    R gv;
+};
+
+// One path sample of the NEE integrator (the conventions the CUDA kernels implement). With
+// `verts`, records every vertex for the adjoint.
 template <class R> void nee_sample(const SceneR<R>& s, const CamBasis& cb, const NeeConfig& c, uint32_t x,
-                                   uint32_t y, uint32_t sample, R L[3], uint32_t& sig, double aov[7], Counters& cnt) {
+                                   uint32_t y, uint32_t sample, R L[3], uint32_t& sig, double aov[7], Counters& cnt,
+                                   std::vector<PathVtx<R>>* verts = nullptr) {
     const uint32_t pixel = y * c.width + x;
     uint32_t st = path_key(c.seed, pixel, sample, 0);
     const float jx = random_float(st), jy = random_float(st);
@@ -403,6 +413,8 @@ template <class R> void nee_sample(const SceneR<R>& s, const CamBasis& cb, const
         const float r1 = random_float(rs), r2 = random_float(rs);
         const V3<R> org = x_hit + n * R(c.eps);
         bool nee = false;
+        int vtx_light = -1;
+        R vtx_gv = R(0);
         if (!s.emitters.empty()) {
             const uint32_t ne = static_cast<uint32_t>(s.emitters.size());
             const int l = s.emitters[static_cast<uint32_t>((static_cast<uint64_t>(sel) * ne) >> 32)];
@@ -436,6 +448,8 @@ template <class R> void nee_sample(const SceneR<R>& s, const CamBasis& cb, const
                         const V3<R> le = load3<R>(s.emission + 3ull * l);
                         Lr = Lr + beta * alb * le * g;
                         sig = sig_mix(sig, k_sig_lit);
+                        vtx_light = l;
+                        vtx_gv = g;
                     } else {
                         sig = sig_mix(sig, k_sig_shadowed);
                     }
@@ -443,6 +457,7 @@ template <class R> void nee_sample(const SceneR<R>& s, const CamBasis& cb, const
             }
         }
         if (!nee) sig = sig_mix(sig, k_sig_no_nee);
+        if (verts) verts->push_back(PathVtx<R>{h, vtx_light, vtx_gv});
         const float r3 = random_float(rs), r4 = random_float(rs);
         const V3<R> nd = cosine_sample<R>(n, r3, r4);
         beta = beta * alb;
@@ -738,6 +753,73 @@ ORACLE_API int oracle_render_nee(uint32_t n, const float* v, const float* albedo
                                  out_rays);
     return render_nee<double>(n, v, albedo, emission, cfg, pixels, npix, out_mean, out_samples, out_sig, out_aov,
                               out_rays);
+}
+
+// Analytic gradient of Loss with respect to per-triangle albedo and emission (FP64), for the
+// image I = mean over samples [sample_base, sample_base + spp) and grad_image = dLoss/dI
+// (w*h*3, top row first). For each path with vertices k on triangles h_k, NEE lights l_k and
+// factors gv_k (g times visibility), beta_k = prod_{j<k} rho_j, d = grad_image(p) / spp:
+//   dLoss/dLe(h_1) += d;  dLoss/dLe(l_k) += d beta_k rho_k gv_k;
+//   dLoss/drho(h_k) += d beta_k H_k with H_k = Le(l_k) gv_k + rho_{k+1} H_{k+1}.
+ORACLE_API int oracle_backward(uint32_t n, const float* v, const float* albedo, const float* emission,
+                               const OracleConfig* cfg, const double* grad_image, double* grad_albedo,
+                               double* grad_emission) {
+    if (!cfg || !grad_image || !grad_albedo || !grad_emission || cfg->spp == 0) return -1;
+    Lbvh b;
+    build_lbvh(n, v, b);
+    SceneR<double> s;
+    prepare(s, n, v, albedo, emission, b);
+    const CamBasis cb = camera_basis(cfg->cam_pos, cfg->cam_target, cfg->cam_up, cfg->cam_fov, cfg->width, cfg->height);
+    const NeeConfig c{cfg->width, cfg->height, cfg->spp, cfg->sample_base, cfg->max_depth, cfg->seed,
+                      cfg->ray_eps > 0.f ? cfg->ray_eps : 1e-4f};
+    const uint32_t threads = std::max<uint32_t>(1, cfg->threads);
+    std::vector<std::vector<double>> ga(threads, std::vector<double>(3ull * n, 0.0)), ge = ga;
+    std::vector<Counters> cnt(threads);
+    parallel_for(c.width * c.height, threads, [&](uint32_t pix, uint32_t tid) {
+        const uint32_t x = pix % c.width, y = pix / c.width;
+        double d[3];
+        for (int k = 0; k < 3; ++k) d[k] = grad_image[3ull * pix + k] / double(c.spp);
+        if (d[0] == 0.0 && d[1] == 0.0 && d[2] == 0.0) return;
+        std::vector<PathVtx<double>> verts;
+        for (uint32_t si = 0; si < c.spp; ++si) {
+            verts.clear();
+            double L[3], aov[7];
+            uint32_t sig;
+            nee_sample<double>(s, cb, c, x, y, c.sample_base + si, L, sig, aov, cnt[tid], &verts);
+            if (verts.empty()) continue;
+            for (int k = 0; k < 3; ++k) ge[tid][3ull * verts[0].prim + k] += d[k];
+            const size_t nv = verts.size();
+            std::vector<double> H(3 * nv, 0.0);
+            for (size_t k = nv; k-- > 0;) {
+                for (int ch = 0; ch < 3; ++ch) {
+                    double h = 0.0;
+                    if (verts[k].light >= 0) h = double(emission[3ull * verts[k].light + ch]) * verts[k].gv;
+                    if (k + 1 < nv) h += double(albedo[3ull * verts[k + 1].prim + ch]) * H[3 * (k + 1) + ch];
+                    H[3 * k + ch] = h;
+                }
+            }
+            double beta[3] = {1.0, 1.0, 1.0};
+            for (size_t k = 0; k < nv; ++k) {
+                const int hprim = verts[k].prim;
+                for (int ch = 0; ch < 3; ++ch) {
+                    const double rho = albedo[3ull * hprim + ch];
+                    ga[tid][3ull * hprim + ch] += d[ch] * beta[ch] * H[3 * k + ch];
+                    if (verts[k].light >= 0) ge[tid][3ull * verts[k].light + ch] += d[ch] * beta[ch] * rho * verts[k].gv;
+                    beta[ch] *= rho;
+                }
+            }
+        }
+    });
+    for (size_t i = 0; i < 3ull * n; ++i) {
+        double sa = 0.0, se = 0.0;
+        for (uint32_t t = 0; t < threads; ++t) {
+            sa += ga[t][i];
+            se += ge[t][i];
+        }
+        grad_albedo[i] = sa;
+        grad_emission[i] = se;
+    }
+    return 0;
 }
 
 // Renders the reference integrator (plugin.mm:223-309) over quads for frames

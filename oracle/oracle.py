@@ -55,6 +55,8 @@ def lib() -> C.CDLL:
         L.oracle_render_reference.restype = C.c_int
         L.oracle_render_reference.argtypes = [C.c_uint32, P, P, P, C.POINTER(OracleConfig), P, P]
         L.oracle_hardware_threads.restype = C.c_uint32
+        L.oracle_backward.restype = C.c_int
+        L.oracle_backward.argtypes = [C.c_uint32, P, P, P, C.POINTER(OracleConfig), P, P, P]
         _lib = L
     return _lib
 
@@ -166,6 +168,23 @@ def render_nee(scene, width: int, height: int, spp: int, depth: int, seed: int =
         raise RuntimeError(f"oracle_render_nee failed: {rc}")
     return {"mean": mean, "aov": aov, "samples": samples, "sig": sig,
             "rays": {"camera": int(rays[0]), "extension": int(rays[1]), "shadow": int(rays[2])}}
+
+
+def backward(scene, width: int, height: int, spp: int, depth: int, grad_image, seed: int = 0,
+             camera: dict | None = None, threads: int | None = None, sample_base: int = 0, eps: float = 1e-4):
+    """FP64 analytic dLoss/dalbedo and dLoss/demission (each (n, 3)) for dLoss/dI = grad_image."""
+    v, a, e = _f32(scene.vertices), _f32(scene.albedo), _f32(scene.emission)
+    cfg = _config(width, height, spp, depth, seed, camera or scene.camera, 64, threads, sample_base, eps)
+    g = np.ascontiguousarray(grad_image, np.float64).reshape(-1)
+    assert g.size == width * height * 3
+    n = v.shape[0]
+    ga = np.zeros((n, 3), np.float64)
+    ge = np.zeros((n, 3), np.float64)
+    rc = lib().oracle_backward(n, v.ctypes.data, a.ctypes.data, e.ctypes.data, C.byref(cfg), g.ctypes.data,
+                               ga.ctypes.data, ge.ctypes.data)
+    if rc:
+        raise RuntimeError(f"oracle_backward failed: {rc}")
+    return ga, ge
 
 
 def render_reference(quads, quad_albedo, quad_emission, width: int, height: int, frames: int, camera: dict,

@@ -87,7 +87,7 @@ class Q_cuda_options(C.Structure):
                 ("integrator", C.c_uint32), ("rebuild_each_frame", C.c_uint32), ("wave_spp", C.c_uint32),
                 ("trace_block", C.c_uint32), ("record_samples", C.c_uint32), ("collect_stats", C.c_uint32),
                 ("profile", C.c_uint32), ("megakernel", C.c_uint32), ("smem_levels", C.c_uint32),
-                ("ray_eps", C.c_float)]
+                ("ray_eps", C.c_float), ("refill_lanes", C.c_uint32), ("trace_steps", C.c_uint32)]
 
 
 class Q_cuda_stats(C.Structure):
@@ -142,4 +142,7 @@ CUDA_SYMBOLS = {
     "Q_cuda_radix_sort_pairs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]),
     "Q_cuda_radix_sort_pairs_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]),
     "Q_cuda_autotune": (C.c_int, [C.c_void_p, C.c_double]),
+    "Q_cuda_set_materials_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32]),
+    "Q_cuda_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
+                                  C.c_void_p]),
 }

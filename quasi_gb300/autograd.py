@@ -1,0 +1,78 @@
+"""torch.autograd binding of the renderer: image = render(albedo, emission).
+
+Forward sets the per-triangle materials from device tensors (Q_cuda_set_materials_device),
+renders `spp` samples per pixel through the plugin and resolves the mean HDR image into a
+torch tensor. Backward calls the path-replay adjoint (Q_cuda_backward), which regenerates
+the same paths from their RNG keys and returns dLoss/dalbedo and dLoss/demission.
+
+Every plugin call is issued on torch's current CUDA stream, so the tensors it reads and
+writes are ordered with the surrounding torch work without extra synchronisation. torch's
+default stream has the handle 0, which the plugin ABI reads as "use your own stream"; it is
+passed as cudaStreamLegacy (1) instead.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from .host import PluginHost, QuasiError
+
+CUDA_STREAM_LEGACY = 1
+
+
+def torch_stream_handle() -> int:
+    """cudaStream_t of torch's current stream, usable by the plugin (never 0)."""
+    return torch.cuda.current_stream().cuda_stream or CUDA_STREAM_LEGACY
+
+
+def _check(host: PluginHost, call: str, rc: int) -> None:
+    if rc != 0:
+        raise QuasiError(call, rc, host.lib.Q_cuda_last_error(host.handle).decode(errors="replace"))
+
+
+class RenderFunction(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, albedo: torch.Tensor, emission: torch.Tensor, host: PluginHost, width: int, height: int,
+                spp: int, sample_base: int):
+        if not (albedo.is_cuda and emission.is_cuda):
+            raise ValueError("albedo and emission must be CUDA tensors")
+        a = albedo.detach().float().contiguous()
+        e = emission.detach().float().contiguous()
+        n = a.shape[0]
+        lib = host.lib
+        _check(host, "Q_cuda_set_materials_device",
+               lib.Q_cuda_set_materials_device(host.handle, C.c_void_p(a.data_ptr()), C.c_void_p(e.data_ptr()), n))
+        host.set_options(spp_per_frame=spp)
+        host.render(width, height, dirty=True, stream=torch_stream_handle())
+        out = torch.empty((height, width, 4), dtype=torch.float32, device=albedo.device)
+        _check(host, "Q_cuda_resolve_device", lib.Q_cuda_resolve_device(host.handle, C.c_void_p(out.data_ptr())))
+        ctx.host, ctx.spp, ctx.sample_base, ctx.n = host, spp, sample_base, n
+        ctx.keep = (a, e)
+        return out[..., :3]
+
+    @staticmethod
+    def backward(ctx, grad_image: torch.Tensor):
+        host = ctx.host
+        g = grad_image.detach().float().contiguous()
+        ga = torch.empty((ctx.n, 3), dtype=torch.float32, device=g.device)
+        ge = torch.empty((ctx.n, 3), dtype=torch.float32, device=g.device)
+        _check(host, "Q_cuda_backward",
+               host.lib.Q_cuda_backward(host.handle, C.c_void_p(g.data_ptr()), ctx.spp, ctx.sample_base,
+                                        C.c_void_p(ga.data_ptr()), C.c_void_p(ge.data_ptr()),
+                                        C.c_void_p(torch_stream_handle())))
+        return ga, ge, None, None, None, None, None
+
+
+def make_host(scene, width: int, height: int, max_depth: int = 4, seed: int = 0, **options) -> PluginHost:
+    """A plugin instance on torch's current stream with `scene` loaded (NEE integrator)."""
+    host = PluginHost(stream=torch_stream_handle(), width=width, height=height)
+    host.set_scene(scene)
+    host.set_options(max_depth=max_depth, seed=seed, **options)
+    return host
+
+
+def render(albedo: torch.Tensor, emission: torch.Tensor, host: PluginHost, width: int, height: int, spp: int,
+           sample_base: int = 0) -> torch.Tensor:
+    """Differentiable render: returns the (height, width, 3) mean image of `spp` samples."""
+    return RenderFunction.apply(albedo, emission, host, width, height, spp, sample_base)

@@ -314,9 +314,53 @@ __global__ void __launch_bounds__(256) k_leaf_boxes(const float4* __restrict__ t
     }
 }
 
+// Copies the first `count` internal nodes in breadth-first order (the top levels of the
+// tree) into `tree`, rewriting child links that stay inside the copy to k_tree_flag | slot.
+// One thread: count is at most a few hundred. The queue of global indices lives in the
+// (not yet written) n3.z words of the output slots.
+__global__ void k_treelet(const float4* __restrict__ nodes, int count, float4* __restrict__ tree) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    constexpr int flag = 0x40000000;
+    tree[3] = make_float4(0.f, 0.f, __int_as_float(0), 0.f);
+    int tail = 1;
+    for (int head = 0; head < tail; ++head) {
+        const int g = __float_as_int(tree[4 * head + 3].z);
+        const float4 n3 = nodes[4 * g + 3];
+        int c[2] = {__float_as_int(n3.x), __float_as_int(n3.y)};
+        for (int k = 0; k < 2; ++k) {
+            if (c[k] >= 0 && tail < count) {
+                tree[4 * tail + 3] = make_float4(0.f, 0.f, __int_as_float(c[k]), 0.f);
+                c[k] = flag | tail;
+                ++tail;
+            }
+        }
+        tree[4 * head + 0] = nodes[4 * g + 0];
+        tree[4 * head + 1] = nodes[4 * g + 1];
+        tree[4 * head + 2] = nodes[4 * g + 2];
+        tree[4 * head + 3] = make_float4(__int_as_float(c[0]), __int_as_float(c[1]), __int_as_float(g), 0.f);
+    }
+}
+
 inline uint32_t ceil_div(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
 
 }  // namespace
+
+cudaError_t LbvhBuilder::build_treelet(int max_nodes, cudaStream_t stream, KernelProfiler& prof) {
+    tree_n_ = 0;
+    if (n_ == 0 || max_nodes <= 0) return cudaSuccess;
+    const int internal = static_cast<int>(n_ > 1 ? n_ - 1 : 1);
+    const int count = std::min(max_nodes, internal);
+    if (count > tree_capacity_) {
+        if (tree_) cudaFree(tree_);
+        tree_ = nullptr;
+        tree_capacity_ = 0;
+        QUASI_TRY_CUDA(cudaMalloc(&tree_, sizeof(float4) * 4 * count));
+        tree_capacity_ = count;
+    }
+    QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_treelet", stream, (k_treelet<<<1, 32, 0, stream>>>(nodes_, count, tree_))));
+    tree_n_ = count;
+    return cudaSuccess;
+}
 
 // ---------------------------------------------------------------- host: radix sort
 
@@ -396,6 +440,9 @@ void LbvhBuilder::release() {
     morton_ = keys_ = order_ = flags_ = nullptr;
     parent_ = nullptr;
     nodes_ = tris_ = nullptr;
+    if (tree_) cudaFree(tree_);
+    tree_ = nullptr;
+    tree_n_ = tree_capacity_ = 0;
     radix_sort_release(sort_);
     capacity_ = 0;
     n_ = 0;

@@ -45,6 +45,8 @@ struct LbvhView {
     const float4* tris = nullptr;   // 3 float4 per triangle in leaf order
     uint32_t tri_count = 0;
     uint32_t node_count = 0;
+    const float4* tree = nullptr;   // top levels in breadth-first order (for shared memory)
+    int tree_n = 0;                 // nodes in `tree`
 };
 
 class LbvhBuilder {
@@ -61,7 +63,12 @@ public:
     // err: device word that receives QUASI_DEVERR_* bits if the hierarchy is malformed.
     cudaError_t build(const float4* tri_in, uint32_t n, cudaStream_t stream, KernelProfiler& prof, uint32_t* err);
 
-    LbvhView view() const { return LbvhView{nodes_, tris_, n_, n_ == 0 ? 0u : (n_ > 1 ? n_ - 1 : 1u)}; }
+    // Copies the top max_nodes internal nodes (breadth first) for staging in shared memory.
+    cudaError_t build_treelet(int max_nodes, cudaStream_t stream, KernelProfiler& prof);
+
+    LbvhView view() const {
+        return LbvhView{nodes_, tris_, n_, n_ == 0 ? 0u : (n_ > 1 ? n_ - 1 : 1u), tree_, tree_n_};
+    }
 
     // Debug copies to host (stream-synchronous).
     cudaError_t read(uint32_t* morton, uint32_t* order, int32_t* children, float* boxes,
@@ -79,6 +86,9 @@ private:
     uint32_t* flags_ = nullptr;      // arrival counters, n-1
     float4* nodes_ = nullptr;
     float4* tris_ = nullptr;
+    float4* tree_ = nullptr;
+    int tree_n_ = 0;
+    int tree_capacity_ = 0;
     RadixSortScratch sort_;
 };
 

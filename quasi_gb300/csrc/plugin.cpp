@@ -287,6 +287,20 @@ Q_CUDA_EXPORT int Q_cuda_resolve_device(Q_plugin_handle* handle, float* device_r
     return r->resolve_device(device_rgba);
 }
 
+Q_CUDA_EXPORT int Q_cuda_set_materials_device(Q_plugin_handle* handle, const float* device_albedo,
+                                              const float* device_emission, uint32_t tri_count) {
+    Q_STATE_OR_FAIL(handle);
+    return r->set_materials_device(device_albedo, device_emission, tri_count);
+}
+
+Q_CUDA_EXPORT int Q_cuda_backward(Q_plugin_handle* handle, const float* device_grad_image, uint32_t spp,
+                                  uint32_t sample_base, float* device_grad_albedo, float* device_grad_emission,
+                                  void* stream) {
+    Q_STATE_OR_FAIL(handle);
+    return r->backward(device_grad_image, spp, sample_base, device_grad_albedo, device_grad_emission,
+                       static_cast<cudaStream_t>(stream));
+}
+
 Q_CUDA_EXPORT int Q_cuda_autotune(Q_plugin_handle* handle, double budget_ms) {
     Q_STATE_OR_FAIL(handle);
     return r->autotune(budget_ms);

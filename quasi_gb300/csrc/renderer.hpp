@@ -15,6 +15,8 @@
 
 namespace quasi {
 
+struct FrameParams;  // device launch parameters (wavefront_kernels.cuh)
+
 struct DeviceBuffer {
     void* ptr = nullptr;
     size_t bytes = 0;
@@ -58,6 +60,14 @@ public:
     int stats(Q_cuda_stats* out);
     int kernel_times(Q_cuda_kernel_time* out, uint32_t capacity, uint32_t* count);
     int autotune(double budget_ms);
+    // Device materials (3 floats per triangle); the set of emitters stays as last set from
+    // host arrays.
+    int set_materials_device(const float* albedo, const float* emission, uint32_t tri_count);
+    // Path-replay adjoint of samples [sample_base, sample_base + spp) of the current frame.
+    int backward(const float* grad_image, uint32_t spp, uint32_t sample_base, float* grad_albedo,
+                 float* grad_emission, cudaStream_t stream);
+    uint32_t tri_count() const { return n_tris_; }
+    uint32_t samples() const { return samples_; }
 
     uint32_t width() const { return width_; }
     uint32_t height() const { return height_; }
@@ -78,9 +88,13 @@ private:
     int render_megakernel(cudaStream_t s, uint32_t spp);
     int render_reference(cudaStream_t s, uint32_t spp);
     uint32_t effective_wave_spp(uint32_t spp) const;
+    FrameParams frame_params(uint32_t spp, uint32_t slots, uint32_t tiles_x) const;
+    bool last_frame_megakernel_ = false;
+    uint64_t mk_paths_ = 0;
 
     int device_ = 0;
-    cudaStream_t stream_ = nullptr;
+    cudaStream_t stream_ = nullptr;        // stream of the most recent call
+    cudaStream_t owned_stream_ = nullptr;  // created by init() when the host gave none
     bool own_stream_ = false;
     int sm_count_ = 0;
     std::string error_;

@@ -1,0 +1,134 @@
+// shading.cuh - one path vertex of the NEE integrator, shared by the wavefront shade kernel,
+// the one-thread-per-path megakernel and the adjoint replay so all three take identical
+// decisions and produce identical values for a given (seed, pixel, sample, bounce).
+//
+// Per vertex k of a path (hit triangle h, incoming double-float ray ro + t rd):
+//   x   = plane(h) intersected with the double-float ray        (hit point)
+//   n   = normalize(cross(e1, e2)) flipped to face the ray       (plugin.mm:192)
+//   key = path_key(seed, pixel, sample, k);  sel = pcg(key); r1, r2, r3, r4 chained
+//   NEE: light l = emitters[(sel * n_emit) >> 32], point y = v0 + su(1-r2) e1 + su r2 e2,
+//        su = sqrt(r1); g = cos_x cos_l / d^2 * area * n_emit / pi, skipped when l == h or a
+//        cosine or d^2 is not positive; the shadow ray runs from y (lifted along the light
+//        normal towards x) to just short of x + eps n.
+//   continuation: cosine-weighted direction from (r3, r4) about n (plugin.mm:111-125),
+//        origin x + eps n.
+// The contribution of the NEE sample is beta * albedo(h) * emission(l) * g when unoccluded.
+#pragma once
+
+#include "common.cuh"
+#include "ffmath.cuh"
+#include "trace.cuh"
+
+namespace quasi {
+
+struct VertexScene {
+    const float4* tri_in;   // original order, v0 v1 v2
+    const float4* albedo;
+    const float4* emission;
+    const int* emitters;
+    uint32_t n_emit;
+    float eps;
+};
+
+struct VertexResult {
+    float3 nrm;        // shading normal (float), facing the incoming ray
+    bool nee;          // a shadow ray is wanted
+    int light;         // emitter triangle of the NEE sample
+    float g;           // NEE factor: contribution = beta * albedo * emission(light) * g
+    float3 so, sd;     // shadow ray origin and unit direction (float)
+    float stmax;       // shadow ray t_max
+    ff3 org;           // continuation origin x + eps n (double-float)
+    ff3 dir;           // continuation direction (valid when want_dir)
+};
+
+// hit: (t, prim, u, v) from the FP32 traversal; ro, rd: the double-float ray that found it.
+__device__ __forceinline__ void shade_vertex(const VertexScene& s, uint32_t key, int prim, float4 hit, const ff3& ro,
+                                             const ff3& rd, bool want_dir, VertexResult& out) {
+    const float3 a = xyz(__ldg(&s.tri_in[3 * prim]));
+    const ff3 e1 = ff3_diff(xyz(__ldg(&s.tri_in[3 * prim + 1])), a);
+    const ff3 e2 = ff3_diff(xyz(__ldg(&s.tri_in[3 * prim + 2])), a);
+    const ff3 ng = ff3_cross(e1, e2);
+    // Re-intersect the hit triangle's plane with the double-float ray.
+    const ff den = ff3_dot(ng, rd);
+    ff3 x;
+    if (den.hi != 0.0f) {
+        const ff t = ff_div(ff3_dot(ng, ff3_sub(ff3v(a), ro)), den);
+        x = ff3_add(ro, ff3_scale(rd, t));
+    } else {
+        x = ff3v(a + ff3_f(e1) * hit.z + ff3_f(e2) * hit.w);
+    }
+    ff3 nrm = ff3_normalize(ng);
+    if (den.hi > 0.0f) nrm = ff3_neg(nrm);
+    out.nrm = ff3_f(nrm);
+    uint32_t st = key;
+    const uint32_t sel = pcg_hash(st);
+    st = sel;
+    const float r1 = rng_next(st);
+    const float r2 = rng_next(st);
+    out.org = ff3_add(x, ff3_scale(nrm, s.eps));
+    out.nee = false;
+    out.light = -1;
+    out.g = 0.0f;
+    if (s.n_emit > 0) {
+        const int l = __ldg(&s.emitters[static_cast<uint32_t>((static_cast<uint64_t>(sel) * s.n_emit) >> 32)]);
+        if (l != prim) {
+            const float3 la = xyz(__ldg(&s.tri_in[3 * l]));
+            const ff3 le1 = ff3_diff(xyz(__ldg(&s.tri_in[3 * l + 1])), la);
+            const ff3 le2 = ff3_diff(xyz(__ldg(&s.tri_in[3 * l + 2])), la);
+            const ff su = ff_sqrt(ffv(r1));
+            const ff3 yl = ff3_add(ff3_add(ff3v(la), ff3_scale(le1, ff_mul(su, two_sum(1.0f, -r2)))),
+                                   ff3_scale(le2, ff_mul(su, r2)));
+            // (y - x) first: both lie on their planes, so a small surface-to-light gap keeps its
+            // digits; subtracting the rounded offset origin would not.
+            const ff3 dv = ff3_sub(ff3_sub(yl, x), ff3_scale(nrm, s.eps));
+            const ff d2 = ff3_dot(dv, dv);
+            const ff dist = ff_sqrt(d2);
+            const ff3 wi = ff3_scale(dv, ff_div(ffv(1.0f), dist));
+            const ff cos_x = ff3_dot(nrm, wi);
+            const ff3 nl = ff3_cross(le1, le2);
+            const ff area2 = ff3_length(nl);
+            const ff cl = ff3_dot(nl, wi);
+            const float cos_l = fabsf(ff_f(ff_div(cl, area2)));
+            if (cos_x.hi > 0.0f && cos_l > 0.0f && d2.hi > 0.0f) {
+                out.g = ff_f(cos_x) * cos_l / ff_f(d2) * (0.5f * ff_f(area2)) * static_cast<float>(s.n_emit) * k_inv_pi;
+                // The shadow ray runs from the light sample, lifted by eps along the light's
+                // normal towards the shading side, to just short of the lifted shading point:
+                // neither end's plane (nor a coplanar neighbour) can be crossed.
+                const float side = cl.hi < 0.0f ? s.eps : -s.eps;
+                const ff3 so = ff3_add(yl, ff3_scale(nl, ff_div(ffv(side), area2)));
+                const ff3 sd = ff3_sub(out.org, so);
+                const ff sdist = ff3_length(sd);
+                out.so = ff3_f(so);
+                out.sd = ff3_f(ff3_scale(sd, ff_div(ffv(1.0f), sdist)));
+                out.stmax = ff_f(sdist) * (1.0f - 1e-4f);
+                out.light = l;
+                out.nee = true;
+            }
+        }
+    }
+    const float r3 = rng_next(st);
+    const float r4 = rng_next(st);
+    if (want_dir) {
+        // plugin.mm:111-125 in double-float: phi = 2 pi r3, cos = sqrt(1 - r4), sin = sqrt(r4).
+        ff sphi, cphi;
+        ff_sincospi(2.0f * r3, sphi, cphi);
+        const ff cos_t = ff_sqrt(two_sum(1.0f, -r4));
+        const ff sin_t = ff_sqrt(ffv(r4));
+        // v = normalize(cross(w, a)), a = (0,1,0) if |w.x| > 0.9 else (1,0,0)
+        ff3 vv = fabsf(nrm.x.hi) > 0.9f ? ff3{ff_neg(nrm.z), ffv(0.0f), nrm.x} : ff3{ffv(0.0f), nrm.z, ff_neg(nrm.y)};
+        vv = ff3_normalize(vv);
+        const ff3 uu = ff3_cross(nrm, vv);
+        out.dir = ff3_normalize(ff3_add(ff3_add(ff3_scale(uu, ff_mul(cphi, sin_t)), ff3_scale(vv, ff_mul(sphi, sin_t))),
+                                        ff3_scale(nrm, cos_t)));
+    }
+}
+
+// First-hit AOVs (plugin.mm:242-249, 301): albedo (emission for emitters), depth, normal.
+__device__ __forceinline__ void first_hit_aovs(float3 alb, float3 em, float t, float3 nrm, float4& aov_a, float4& aov_n) {
+    const float3 aa = max3(em) > 0.1f ? em : alb;
+    const float depth = fminf(fmaxf((t - 1.0f) * 0.25f, 0.0f), 1.0f);
+    aov_a = make_float4(aa.x, aa.y, aa.z, depth);
+    aov_n = make_float4(nrm.x * 0.5f + 0.5f, nrm.y * 0.5f + 0.5f, nrm.z * 0.5f + 0.5f, 0.f);
+}
+
+}  // namespace quasi

@@ -3,6 +3,7 @@
 // kernels are in wavefront_kernels.cuh.
 #include "renderer.hpp"
 #include "wavefront_kernels.cuh"
+#include "megakernel.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -79,7 +80,10 @@ Renderer::~Renderer() {
     if (err_host_) cudaFreeHost(err_host_);
     for (cudaEvent_t e : {ev_frame0_, ev_frame1_, ev_bvh0_, ev_bvh1_})
         if (e) cudaEventDestroy(e);
-    if (own_stream_ && stream_) cudaStreamDestroy(stream_);
+    if (owned_stream_) {
+        cudaStreamSynchronize(owned_stream_);
+        cudaStreamDestroy(owned_stream_);
+    }
 }
 
 int Renderer::cuda_fail(cudaError_t e, const char* where) {
@@ -97,8 +101,8 @@ int Renderer::init() {
     R_TRY(cudaSetDevice(device_), "cudaSetDevice");
     R_TRY(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device_), "sm count");
     if (!stream_) {
-        R_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream");
-        own_stream_ = true;
+        R_TRY(cudaStreamCreateWithFlags(&owned_stream_, cudaStreamNonBlocking), "stream");
+        stream_ = owned_stream_;
     }
     R_TRY(cudaEventCreate(&ev_frame0_), "event");
     R_TRY(cudaEventCreate(&ev_frame1_), "event");
@@ -203,6 +207,9 @@ int Renderer::set_options(const Q_cuda_options& o) {
     if (!(n.ray_eps > 0.f)) n.ray_eps = 1e-4f;
     if (n.trace_block != 0 && (n.trace_block % 32 != 0 || n.trace_block > 256))
         return fail(QUASI_ERR_INVALID, "trace_block must be a multiple of 32 up to 256");
+    if (n.refill_lanes > 32) return fail(QUASI_ERR_INVALID, "refill_lanes must be at most 32");
+    if (n.smem_levels > 9 && n.smem_levels != 32)
+        return fail(QUASI_ERR_INVALID, "smem_levels must be 0 (default), 1..9, or 32 (none)");
     const bool changed = n.seed != opt_.seed || n.max_depth != opt_.max_depth || n.integrator != opt_.integrator ||
                          n.ray_eps != opt_.ray_eps;
     opt_ = n;
@@ -280,6 +287,8 @@ int Renderer::render(const Q_render_frame& fr) {
     if (opt_.integrator == QUASI_INTEGRATOR_NEE && (bvh_dirty_ || opt_.rebuild_each_frame)) {
         R_TRY(cudaEventRecord(ev_bvh0_, s), "event");
         R_TRY(bvh_.build(tri_in_.as<float4>(), n_tris_, s, prof_, err_dev_.as<uint32_t>()), "lbvh build");
+        const int levels = opt_.smem_levels ? static_cast<int>(opt_.smem_levels) : k_default_smem_levels;
+        R_TRY(bvh_.build_treelet(levels >= 31 ? 0 : (1 << levels) - 1, s, prof_), "treelet");
         R_TRY(cudaEventRecord(ev_bvh1_, s), "event");
         bvh_timed_ = true;
         bvh_dirty_ = false;
@@ -292,6 +301,7 @@ int Renderer::render(const Q_render_frame& fr) {
         record_spp_ = spp;
     }
     if (opt_.integrator == QUASI_INTEGRATOR_REFERENCE) rc = render_reference(s, spp);
+    else if (opt_.megakernel) rc = render_megakernel(s, spp);
     else rc = render_wavefront(s, spp);
     if (rc) return rc;
     samples_ += spp;
@@ -331,7 +341,15 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
 
     const LbvhView bv = bvh_.view();
     SceneDev sd{tri_in_.as<float4>(), albedo_.as<float4>(), emission_.as<float4>(), emitters_.as<int>(),
-                bv.nodes, bv.tris, n_tris_, n_emit_};
+                bv.nodes,
+                bv.tris,
+                n_tris_,
+                n_emit_,
+                opt_.refill_lanes ? static_cast<int>(opt_.refill_lanes) : k_refill_lanes,
+                opt_.trace_steps ? static_cast<int>(opt_.trace_steps) : k_trace_steps,
+                bv.tree,
+                bv.tree_n};
+    const size_t tree_smem = sizeof(float4) * 4 * static_cast<size_t>(sd.tree_n);
     PathDev pd{beta_.as<float4>(),  lpath_.as<float4>(), aov_a_.as<float4>(),
                aov_n_.as<float4>(), ray_ff_.as<float4>(), opt_.record_samples ? sig_.as<uint32_t>() : nullptr};
     FrameParams f{};
@@ -346,14 +364,24 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
     f.frame_spp = spp;
 
     const int tb = opt_.trace_block ? static_cast<int>(opt_.trace_block) : 128;
+    using ClosestFn = void (*)(SceneDev, const float4*, float4*, const int*, int, int*, uint32_t*, unsigned long long*);
+    using ShadowFn = void (*)(SceneDev, PathDev, const float4*, const int*, int, int*, uint32_t*, unsigned long long*);
+    const int mode = sd.refill < 32 ? k_mode_refill : (sd.tree_n > 0 ? k_mode_batch_tree : k_mode_batch);
+    static const ClosestFn closest_fns[2][3] = {
+        {k_trace_closest<false, k_mode_batch>, k_trace_closest<false, k_mode_batch_tree>,
+         k_trace_closest<false, k_mode_refill>},
+        {k_trace_closest<true, k_mode_batch>, k_trace_closest<true, k_mode_batch_tree>,
+         k_trace_closest<true, k_mode_refill>}};
+    static const ShadowFn shadow_fns[2][3] = {
+        {k_trace_shadow<false, k_mode_batch>, k_trace_shadow<false, k_mode_batch_tree>,
+         k_trace_shadow<false, k_mode_refill>},
+        {k_trace_shadow<true, k_mode_batch>, k_trace_shadow<true, k_mode_batch_tree>,
+         k_trace_shadow<true, k_mode_refill>}};
+    const ClosestFn kc = closest_fns[opt_.collect_stats ? 1 : 0][mode];
+    const ShadowFn ks = shadow_fns[opt_.collect_stats ? 1 : 0][mode];
     int occ_c = 0, occ_s = 0;
-    if (opt_.collect_stats) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, k_trace_closest<true>, tb, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_trace_shadow<true>, tb, 0);
-    } else {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, k_trace_closest<false>, tb, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, k_trace_shadow<false>, tb, 0);
-    }
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, kc, tb, tree_smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, ks, tb, tree_smem);
     const int grid_c = sm_count_ * std::max(occ_c, 1);
     const int grid_s = sm_count_ * std::max(occ_s, 1);
     const int grid_shade = sm_count_ * 8;
@@ -379,31 +407,19 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
             int* c_shadow = cnt + D + (k - 1);
             int* f_cur = cnt + 2 * D + (k - 1);
             int* f_shadow = cnt + 3 * D + (k - 1);
-            if (opt_.collect_stats)
-                R_TRY(QUASI_LAUNCH(prof_, "trace_closest", s,
-                                   (k_trace_closest<true><<<grid_c, tb, 0, s>>>(sd, qcur, hits_.as<float4>(), c_cur,
-                                                                                cap, f_cur, err, st))),
-                      "trace_closest");
-            else
-                R_TRY(QUASI_LAUNCH(prof_, "trace_closest", s,
-                                   (k_trace_closest<false><<<grid_c, tb, 0, s>>>(sd, qcur, hits_.as<float4>(), c_cur,
-                                                                                 cap, f_cur, err, st))),
-                      "trace_closest");
+            R_TRY(QUASI_LAUNCH(prof_, "trace_closest", s,
+                               (kc<<<grid_c, tb, tree_smem, s>>>(sd, qcur, hits_.as<float4>(), c_cur, cap, f_cur, err,
+                                                                 st))),
+                  "trace_closest");
             R_TRY(QUASI_LAUNCH(prof_, "shade", s,
                                (k_shade<<<grid_shade, 256, 0, s>>>(f, sd, pd, k, qcur, hits_.as<float4>(), c_cur, cap, qnext,
                                                                   k < D ? c_next : nullptr, shadow_.as<float4>(),
                                                                   c_shadow))),
                   "shade");
-            if (opt_.collect_stats)
-                R_TRY(QUASI_LAUNCH(prof_, "trace_shadow", s,
-                                   (k_trace_shadow<true><<<grid_s, tb, 0, s>>>(sd, pd, shadow_.as<float4>(), c_shadow,
-                                                                               cap, f_shadow, err, st))),
-                      "trace_shadow");
-            else
-                R_TRY(QUASI_LAUNCH(prof_, "trace_shadow", s,
-                                   (k_trace_shadow<false><<<grid_s, tb, 0, s>>>(sd, pd, shadow_.as<float4>(), c_shadow,
-                                                                                cap, f_shadow, err, st))),
-                      "trace_shadow");
+            R_TRY(QUASI_LAUNCH(prof_, "trace_shadow", s,
+                               (ks<<<grid_s, tb, tree_smem, s>>>(sd, pd, shadow_.as<float4>(), c_shadow, cap, f_shadow,
+                                                                 err, st))),
+                  "trace_shadow");
         }
         R_TRY(QUASI_LAUNCH(prof_, "accumulate", s,
                            (k_accumulate<<<ceil_div(px, 256), 256, 0, s>>>(
@@ -416,11 +432,131 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
     R_TRY(cudaMemcpyAsync(counters_host_, counters_.ptr, sizeof(int) * need, cudaMemcpyDeviceToHost, s), "d2h");
     R_TRY(cudaMemcpyAsync(stats_host_, stats_dev_.ptr, sizeof(unsigned long long) * 5, cudaMemcpyDeviceToHost, s), "d2h");
     R_TRY(cudaMemcpyAsync(err_host_, err_dev_.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, s), "d2h");
+    last_frame_megakernel_ = false;
     stats_pending_ = true;
     return QUASI_OK;
 }
 
-int Renderer::render_megakernel(cudaStream_t, uint32_t) { return fail(QUASI_ERR_INVALID, "megakernel not built"); }
+SceneDev Renderer_scene_dev(const LbvhView& bv, const DeviceBuffer& tri_in, const DeviceBuffer& albedo,
+                            const DeviceBuffer& emission, const DeviceBuffer& emitters, uint32_t n_tris, uint32_t n_emit) {
+    return SceneDev{tri_in.as<float4>(), albedo.as<float4>(), emission.as<float4>(), emitters.as<int>(), bv.nodes,
+                    bv.tris, n_tris, n_emit, k_refill_lanes, k_trace_steps, nullptr, 0};
+}
+
+FrameParams Renderer::frame_params(uint32_t spp, uint32_t slots, uint32_t tiles_x) const {
+    FrameParams f{};
+    f.cam = make_camera_basis(camera_, width_, height_);
+    f.width = width_;
+    f.height = height_;
+    f.tiles_x = tiles_x;
+    f.slots = slots;
+    f.seed = opt_.seed;
+    f.max_depth = opt_.max_depth;
+    f.eps = opt_.ray_eps;
+    f.frame_spp = spp;
+    return f;
+}
+
+// One-thread-per-path renderer: same waves, path ids and accumulation as the wavefront, so
+// its per-sample radiance (and therefore the image) is bit-identical.
+int Renderer::render_megakernel(cudaStream_t s, uint32_t spp) {
+    const uint32_t tiles_x = ceil_div(width_, 8), tiles_y = ceil_div(height_, 4);
+    const uint32_t slots = tiles_x * tiles_y * 32;
+    const uint32_t S = effective_wave_spp(spp);
+    const uint32_t waves = ceil_div(spp, S);
+    int rc = ensure_wave_buffers(slots * S);
+    if (rc) return rc;
+    if (counter_capacity_ < waves + 2) {
+        R_TRY(counters_.reserve(sizeof(int) * (waves + 2)), "counters");
+        if (counters_host_) cudaFreeHost(counters_host_);
+        R_TRY(cudaMallocHost(&counters_host_, sizeof(int) * (waves + 2)), "pinned");
+        counter_capacity_ = waves + 2;
+    }
+    counters_used_ = 0;
+    R_TRY(cudaMemsetAsync(counters_.ptr, 0, sizeof(int) * (waves + 2), s), "memset");
+    R_TRY(cudaMemsetAsync(stats_dev_.ptr, 0, sizeof(unsigned long long) * 4, s), "memset");
+    R_TRY(cudaMemsetAsync(stats_dev_.as<unsigned long long>() + 5, 0, sizeof(unsigned long long) * 2, s), "memset");
+    const SceneDev sd = Renderer_scene_dev(bvh_.view(), tri_in_, albedo_, emission_, emitters_, n_tris_, n_emit_);
+    PathDev pd{beta_.as<float4>(),  lpath_.as<float4>(), aov_a_.as<float4>(),
+               aov_n_.as<float4>(), ray_ff_.as<float4>(), opt_.record_samples ? sig_.as<uint32_t>() : nullptr};
+    FrameParams f = frame_params(spp, slots, tiles_x);
+    int occ = 0;
+    auto kern = opt_.collect_stats ? k_megakernel<true> : k_megakernel<false>;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 128, 0);
+    const int grid = sm_count_ * std::max(occ, 1);
+    unsigned long long* st = stats_dev_.as<unsigned long long>();
+    const uint32_t px = width_ * height_;
+    for (uint32_t w = 0; w < waves; ++w) {
+        f.wave_spp = std::min(S, spp - w * S);
+        f.sample_base = samples_ + w * S;
+        f.wave_offset = w * S;
+        R_TRY(QUASI_LAUNCH(prof_, "megakernel", s,
+                           (kern<<<grid, 128, 0, s>>>(f, sd, pd, counters_.as<int>() + w, err_dev_.as<uint32_t>(), st))),
+              "megakernel");
+        R_TRY(QUASI_LAUNCH(prof_, "accumulate", s,
+                           (k_accumulate<<<ceil_div(px, 256), 256, 0, s>>>(
+                               f, pd, accum_.as<float4>(), comp_.as<float4>(), aov_albedo_.as<float4>(),
+                               aov_normal_.as<float4>(), opt_.record_samples ? record_rad_.as<float>() : nullptr,
+                               opt_.record_samples ? record_sig_.as<uint32_t>() : nullptr))),
+              "accumulate");
+    }
+    R_TRY(cudaMemcpyAsync(stats_host_, stats_dev_.ptr, sizeof(unsigned long long) * 7, cudaMemcpyDeviceToHost, s), "d2h");
+    R_TRY(cudaMemcpyAsync(err_host_, err_dev_.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, s), "d2h");
+    mk_paths_ = static_cast<uint64_t>(px) * spp;
+    last_frame_megakernel_ = true;
+    stats_pending_ = true;
+    return QUASI_OK;
+}
+
+int Renderer::set_materials_device(const float* albedo, const float* emission, uint32_t tri_count) {
+    if (tri_count != n_tris_) return fail(QUASI_ERR_INVALID, "material count differs from the scene");
+    if (tri_count == 0) return QUASI_OK;
+    R_TRY(QUASI_LAUNCH(prof_, "pack_materials", stream_,
+                       (k_pack_materials<<<ceil_div(tri_count, 256), 256, 0, stream_>>>(
+                           albedo, emission, tri_count, albedo_.as<float4>(), emission_.as<float4>()))),
+          "pack_materials");
+    return reset();
+}
+
+int Renderer::backward(const float* grad_image, uint32_t spp, uint32_t sample_base, float* grad_albedo,
+                       float* grad_emission, cudaStream_t stream) {
+    if (stream) stream_ = stream;
+    if (!has_scene_) return fail(QUASI_ERR_STATE, "no scene");
+    if (opt_.integrator != QUASI_INTEGRATOR_NEE) return fail(QUASI_ERR_STATE, "backward needs the NEE integrator");
+    if (!grad_image || !grad_albedo || !grad_emission || spp == 0) return fail(QUASI_ERR_INVALID, "backward arguments");
+    if (opt_.max_depth > static_cast<uint32_t>(k_adjoint_max_depth))
+        return fail(QUASI_ERR_INVALID, "backward supports max_depth up to 16");
+    if (width_ == 0 || height_ == 0) return fail(QUASI_ERR_STATE, "render a frame before backward");
+    cudaStream_t s = stream_;
+    if (bvh_dirty_) {
+        R_TRY(bvh_.build(tri_in_.as<float4>(), n_tris_, s, prof_, err_dev_.as<uint32_t>()), "lbvh build");
+        bvh_dirty_ = false;
+    }
+    R_TRY(cudaMemsetAsync(grad_albedo, 0, sizeof(float) * 3ull * n_tris_, s), "memset");
+    R_TRY(cudaMemsetAsync(grad_emission, 0, sizeof(float) * 3ull * n_tris_, s), "memset");
+    if (counter_capacity_ < 1) {
+        R_TRY(counters_.reserve(sizeof(int) * 4), "counters");
+        if (counters_host_) cudaFreeHost(counters_host_);
+        R_TRY(cudaMallocHost(&counters_host_, sizeof(int) * 4), "pinned");
+        counter_capacity_ = 4;
+    }
+    R_TRY(cudaMemsetAsync(counters_.ptr, 0, sizeof(int), s), "memset");
+    const uint32_t tiles_x = ceil_div(width_, 8), tiles_y = ceil_div(height_, 4);
+    const uint32_t slots = tiles_x * tiles_y * 32;
+    FrameParams f = frame_params(spp, slots, tiles_x);
+    f.wave_spp = spp;
+    f.sample_base = sample_base;
+    f.wave_offset = 0;
+    const SceneDev sd = Renderer_scene_dev(bvh_.view(), tri_in_, albedo_, emission_, emitters_, n_tris_, n_emit_);
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjoint, 128, 0);
+    const int grid = sm_count_ * std::max(occ, 1);
+    R_TRY(QUASI_LAUNCH(prof_, "adjoint", s,
+                       (k_adjoint<<<grid, 128, 0, s>>>(f, sd, grad_image, 1.0f / static_cast<float>(spp), grad_albedo,
+                                                      grad_emission, counters_.as<int>(), err_dev_.as<uint32_t>()))),
+          "adjoint");
+    return QUASI_OK;
+}
 
 int Renderer::render_reference(cudaStream_t s, uint32_t spp) {
     if (n_quads_ == 0) return fail(QUASI_ERR_STATE, "reference integrator needs quads");
@@ -495,7 +631,16 @@ int Renderer::read_bvh(uint32_t* morton, uint32_t* order, int32_t* children, flo
 int Renderer::stats(Q_cuda_stats* out) {
     R_TRY(cudaStreamSynchronize(stream_), "sync");
     Q_cuda_stats st{};
-    if (stats_pending_) {
+    if (stats_pending_ && last_frame_megakernel_) {
+        st.camera_rays = mk_paths_;
+        st.extension_rays = stats_host_[5] - mk_paths_;
+        st.shadow_rays = stats_host_[6];
+        if (opt_.collect_stats) {
+            st.node_visits = stats_host_[0];
+            st.tri_tests = stats_host_[1];
+        }
+        last_stats_ = st;
+    } else if (stats_pending_) {
         const uint32_t D = opt_.max_depth;
         const uint32_t per_wave = 4 * D;
         const uint32_t waves = per_wave ? counters_used_ / per_wave : 0;

@@ -22,6 +22,7 @@
 
 #include "common.cuh"
 #include "ffmath.cuh"
+#include "shading.cuh"
 #include "trace.cuh"
 
 namespace quasi {
@@ -49,7 +50,19 @@ struct SceneDev {
     const float4* nodes;
     const float4* tris;     // leaf order, v0+orig, e1, e2
     uint32_t n_tris, n_emit;
+    int refill;             // idle lanes that trigger a ray refill in the trace kernels
+    int steps;              // node visits per lane between refill checks
+    const float4* tree;     // top BVH levels, breadth first, staged in shared memory
+    int tree_n;             // nodes in `tree` (0 = no staging)
 };
+
+// Copies the treelet into the block's shared memory (dynamic size tree_n * 64 bytes).
+__device__ __forceinline__ const float4* stage_treelet(const SceneDev& s) {
+    extern __shared__ float4 s_tree[];
+    for (int i = threadIdx.x; i < 4 * s.tree_n; i += blockDim.x) s_tree[i] = __ldg(&s.tree[i]);
+    __syncthreads();
+    return s_tree;
+}
 
 struct PathDev {
     float4* beta;
@@ -141,66 +154,90 @@ __device__ __forceinline__ void flush_counters(const TraceCounters& c, unsigned 
     }
 }
 
-// Persistent closest-hit traversal: warps grab 32 rays at a time from the queue.
-template <bool STATS>
+// Closest-hit queue: ray i is q[2i] = (origin, path id), q[2i+1] = (direction, excluded
+// triangle); the result is hits[i] = (t, triangle or -1, u, v).
+struct ClosestJob {
+    const float4* __restrict__ q;
+    float4* __restrict__ hits;
+    __device__ __forceinline__ void load(int i, float3& o, float3& d, float& tmax, int& exclude) const {
+        const float4 r0 = q[2 * i], r1 = q[2 * i + 1];
+        o = xyz(r0);
+        d = xyz(r1);
+        tmax = __int_as_float(0x7f800000);
+        exclude = __float_as_int(r1.w);
+    }
+    __device__ __forceinline__ void store(int i, const TraceState& s) const {
+        hits[i] = make_float4(s.best_t, __int_as_float(s.best), s.bu, s.bv);
+    }
+};
+
+// Shadow queue: sq[3i] = (origin, path id), sq[3i+1] = (direction, t_max), sq[3i+2] =
+// (contribution); an unoccluded ray adds its contribution to the path's radiance.
+struct ShadowJob {
+    const float4* __restrict__ sq;
+    PathDev p;
+    __device__ __forceinline__ void load(int i, float3& o, float3& d, float& tmax, int& exclude) const {
+        const float4 r0 = sq[3 * i], r1 = sq[3 * i + 1];
+        o = xyz(r0);
+        d = xyz(r1);
+        tmax = r1.w;
+        exclude = -1;
+    }
+    __device__ __forceinline__ void store(int i, const TraceState& s) const {
+        const int pid = __float_as_int(sq[3 * i].w);
+        if (s.best < 0) {
+            const float4 c = sq[3 * i + 2];
+            float4 L = p.lpath[pid];
+            L.x += c.x;
+            L.y += c.y;
+            L.z += c.z;
+            p.lpath[pid] = L;
+        }
+        if (p.sig) p.sig[pid] = sig_mix(p.sig[pid], s.best < 0 ? k_sig_lit : k_sig_shadowed);
+    }
+};
+
+// Traversal modes of the persistent trace kernels.
+constexpr int k_mode_batch = 0;       // warp batches of 32 rays, nodes from global memory
+constexpr int k_mode_batch_tree = 1;  // warp batches, top levels from shared memory
+constexpr int k_mode_refill = 2;      // per-lane refill (trace_persistent)
+
+// Persistent closest-hit traversal.
+template <bool STATS, int MODE>
 __global__ void __launch_bounds__(256) k_trace_closest(SceneDev s, const float4* __restrict__ q,
                                                        float4* __restrict__ hits, const int* __restrict__ count,
                                                        int capacity, int* __restrict__ fetch,
                                                        uint32_t* __restrict__ err, unsigned long long* __restrict__ stats) {
     const int n = min(*count, capacity);
-    const int lane = threadIdx.x & 31;
     uint32_t e = 0;
     TraceCounters c;
-    while (true) {
-        int base = 0;
-        if (lane == 0) base = atomicAdd(fetch, 32);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n) break;
-        const int i = base + lane;
-        if (i < n) {
-            const float4 r0 = q[2 * i], r1 = q[2 * i + 1];
-            const RayInv r = make_ray(xyz(r0), xyz(r1));
-            float t, bu, bv;
-            const int prim = trace_bvh<false, STATS>(s.nodes, s.tris, s.n_tris, r, __int_as_float(0x7f800000),
-                                                     __float_as_int(r1.w), t, bu, bv, e, c);
-            hits[i] = make_float4(t, __int_as_float(prim), bu, bv);
-        }
-    }
+    ClosestJob job{q, hits};
+    if (MODE == k_mode_refill)
+        trace_persistent<false, STATS>(job, s.nodes, s.tris, s.n_tris, n, s.refill, s.steps, fetch, e, c);
+    else if (MODE == k_mode_batch_tree)
+        trace_batches<false, STATS, true>(job, s.nodes, s.tris, s.n_tris, n, fetch, e, c, stage_treelet(s), s.tree_n);
+    else
+        trace_batches<false, STATS, false>(job, s.nodes, s.tris, s.n_tris, n, fetch, e, c, nullptr, 0);
     if (e) atomicOr(err, e);
     flush_counters<STATS>(c, stats);
 }
 
-template <bool STATS>
+// Persistent any-hit traversal of the shadow queue.
+template <bool STATS, int MODE>
 __global__ void __launch_bounds__(256) k_trace_shadow(SceneDev s, PathDev p, const float4* __restrict__ sq,
                                                       const int* __restrict__ count, int capacity,
                                                       int* __restrict__ fetch, uint32_t* __restrict__ err,
                                                       unsigned long long* __restrict__ stats) {
     const int n = min(*count, capacity);
-    const int lane = threadIdx.x & 31;
     uint32_t e = 0;
     TraceCounters c;
-    while (true) {
-        int base = 0;
-        if (lane == 0) base = atomicAdd(fetch, 32);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n) break;
-        const int i = base + lane;
-        if (i < n) {
-            const float4 r0 = sq[3 * i], r1 = sq[3 * i + 1], r2 = sq[3 * i + 2];
-            const RayInv r = make_ray(xyz(r0), xyz(r1));
-            float t, bu, bv;
-            const int hit = trace_bvh<true, STATS>(s.nodes, s.tris, s.n_tris, r, r1.w, -1, t, bu, bv, e, c);
-            const int pid = __float_as_int(r0.w);
-            if (hit < 0) {
-                float4 L = p.lpath[pid];
-                L.x += r2.x;
-                L.y += r2.y;
-                L.z += r2.z;
-                p.lpath[pid] = L;
-            }
-            if (p.sig) p.sig[pid] = sig_mix(p.sig[pid], hit < 0 ? k_sig_lit : k_sig_shadowed);
-        }
-    }
+    ShadowJob job{sq, p};
+    if (MODE == k_mode_refill)
+        trace_persistent<true, STATS>(job, s.nodes, s.tris, s.n_tris, n, s.refill, s.steps, fetch, e, c);
+    else if (MODE == k_mode_batch_tree)
+        trace_batches<true, STATS, true>(job, s.nodes, s.tris, s.n_tris, n, fetch, e, c, stage_treelet(s), s.tree_n);
+    else
+        trace_batches<true, STATS, false>(job, s.nodes, s.tris, s.n_tris, n, fetch, e, c, nullptr, 0);
     if (e) atomicOr(err, e);
     flush_counters<STATS>(c, stats + 2);
 }
@@ -227,11 +264,14 @@ __global__ void __launch_bounds__(256) k_shade(FrameParams f, SceneDev s, PathDe
     const int n = min(*count, capacity);
     const int lane = threadIdx.x & 31;
     const int stride = gridDim.x * blockDim.x;
+    const VertexScene vs{s.tri_in, s.albedo, s.emission, s.emitters, s.n_emit, f.eps};
     for (int base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; base < n; base += stride) {
         const int i = base + lane;
         bool want_shadow = false, want_next = false;
-        float3 sorg = mk3(0.f, 0.f, 0.f), wi_f = sorg, contrib = sorg, norg = sorg, nd = sorg;
-        float tmax_s = 0.f;
+        float3 contrib = mk3(0.f, 0.f, 0.f), norg = contrib, nd = contrib;
+        VertexResult v;
+        v.so = v.sd = contrib;
+        v.stmax = 0.f;
         int pid = 0, prim = -1;
         if (i < n) {
             const float4 h = hits[i];
@@ -242,110 +282,41 @@ __global__ void __launch_bounds__(256) k_shade(FrameParams f, SceneDev s, PathDe
             } else {
                 ff3 ro, rd;
                 ff_ray_load(&p.ray_ff[3ull * pid], ro, rd);
-                const float3 a = xyz(__ldg(&s.tri_in[3 * prim]));
-                const ff3 e1 = ff3_diff(xyz(__ldg(&s.tri_in[3 * prim + 1])), a);
-                const ff3 e2 = ff3_diff(xyz(__ldg(&s.tri_in[3 * prim + 2])), a);
-                const ff3 ng = ff3_cross(e1, e2);
-                // Re-intersect the hit triangle's plane with the double-float ray.
-                const ff den = ff3_dot(ng, rd);
-                ff3 x;
-                if (den.hi != 0.0f) {
-                    const ff t = ff_div(ff3_dot(ng, ff3_sub(ff3v(a), ro)), den);
-                    x = ff3_add(ro, ff3_scale(rd, t));
-                } else {
-                    x = ff3v(a + ff3_f(e1) * h.z + ff3_f(e2) * h.w);
-                }
-                ff3 nrm = ff3_normalize(ng);
-                if (den.hi > 0.0f) nrm = ff3_neg(nrm);  // face the incoming ray (plugin.mm:192)
-                const float3 nrm_f = ff3_f(nrm);
+                const uint32_t j = static_cast<uint32_t>(pid) / f.slots;
+                uint32_t px, py;
+                slot_to_xy(static_cast<uint32_t>(pid) - j * f.slots, f.tiles_x, px, py);
+                const uint32_t key = path_key(f.seed, py * f.width + px, f.sample_base + j, bounce);
                 const float3 alb = xyz(__ldg(&s.albedo[prim]));
                 float3 beta = xyz(p.beta[pid]);
+                const float3 nb = beta * alb;
+                const bool cont = bounce < f.max_depth && max3(nb) > 0.0f;
+                shade_vertex(vs, key, prim, h, ro, rd, cont, v);
                 uint32_t sig = p.sig ? sig_mix(p.sig[pid], static_cast<uint32_t>(prim)) : 0u;
                 if (bounce == 1) {
                     const float3 em = xyz(__ldg(&s.emission[prim]));
                     p.lpath[pid] = make_float4(em.x, em.y, em.z, 0.f);
-                    const float3 aa = max3(em) > 0.1f ? em : alb;
-                    const float depth = fminf(fmaxf((h.x - 1.0f) * 0.25f, 0.0f), 1.0f);
-                    p.aov_a[pid] = make_float4(aa.x, aa.y, aa.z, depth);
-                    p.aov_n[pid] = make_float4(nrm_f.x * 0.5f + 0.5f, nrm_f.y * 0.5f + 0.5f, nrm_f.z * 0.5f + 0.5f, 0.f);
+                    first_hit_aovs(alb, em, h.x, v.nrm, p.aov_a[pid], p.aov_n[pid]);
                 }
-                const uint32_t j = static_cast<uint32_t>(pid) / f.slots;
-                uint32_t px, py;
-                slot_to_xy(static_cast<uint32_t>(pid) - j * f.slots, f.tiles_x, px, py);
-                uint32_t st = path_key(f.seed, py * f.width + px, f.sample_base + j, bounce);
-                const uint32_t sel = pcg_hash(st);
-                st = sel;
-                const float r1 = rng_next(st);
-                const float r2 = rng_next(st);
-                const ff3 org = ff3_add(x, ff3_scale(nrm, f.eps));
-                if (s.n_emit > 0) {
-                    const int l = __ldg(&s.emitters[static_cast<uint32_t>((static_cast<uint64_t>(sel) * s.n_emit) >> 32)]);
-                    if (l != prim) {
-                        const float3 la = xyz(__ldg(&s.tri_in[3 * l]));
-                        const ff3 le1 = ff3_diff(xyz(__ldg(&s.tri_in[3 * l + 1])), la);
-                        const ff3 le2 = ff3_diff(xyz(__ldg(&s.tri_in[3 * l + 2])), la);
-                        const ff su = ff_sqrt(ffv(r1));
-                        const ff3 yl = ff3_add(ff3_add(ff3v(la), ff3_scale(le1, ff_mul(su, two_sum(1.0f, -r2)))),
-                                               ff3_scale(le2, ff_mul(su, r2)));
-                        const ff3 dv = ff3_sub(ff3_sub(yl, x), ff3_scale(nrm, f.eps));
-                        const ff d2 = ff3_dot(dv, dv);
-                        const ff dist = ff_sqrt(d2);
-                        const ff3 wi = ff3_scale(dv, ff_div(ffv(1.0f), dist));
-                        const ff cos_x = ff3_dot(nrm, wi);
-                        const ff3 nl = ff3_cross(le1, le2);
-                        const ff area2 = ff3_length(nl);
-                        const ff cl = ff3_dot(nl, wi);
-                        const float cos_l = fabsf(ff_f(ff_div(cl, area2)));
-                        if (cos_x.hi > 0.0f && cos_l > 0.0f && d2.hi > 0.0f) {
-                            const float g = ff_f(cos_x) * cos_l / ff_f(d2) * (0.5f * ff_f(area2)) *
-                                            static_cast<float>(s.n_emit) * k_inv_pi;
-                            contrib = beta * alb * xyz(__ldg(&s.emission[l])) * g;
-                            // The shadow ray runs from the light sample, lifted by eps along the
-                            // light's normal towards the shading side, to just short of the lifted
-                            // shading point: neither end's plane (nor a coplanar neighbour) can
-                            // be crossed, however grazing the ray.
-                            const float side = cl.hi < 0.0f ? f.eps : -f.eps;
-                            const ff3 so = ff3_add(yl, ff3_scale(nl, ff_div(ffv(side), area2)));
-                            const ff3 sd = ff3_sub(org, so);
-                            const ff sdist = ff3_length(sd);
-                            sorg = ff3_f(so);
-                            wi_f = ff3_f(ff3_scale(sd, ff_div(ffv(1.0f), sdist)));
-                            tmax_s = ff_f(sdist) * (1.0f - 1e-4f);
-                            want_shadow = true;
-                        }
-                    }
+                if (v.nee) {
+                    contrib = beta * alb * xyz(__ldg(&s.emission[v.light])) * v.g;
+                    want_shadow = true;
+                } else {
+                    sig = sig_mix(sig, k_sig_no_nee);
                 }
-                if (!want_shadow) sig = sig_mix(sig, k_sig_no_nee);
-                const float r3 = rng_next(st);
-                const float r4 = rng_next(st);
-                beta = beta * alb;
-                p.beta[pid] = make_float4(beta.x, beta.y, beta.z, 0.f);
+                p.beta[pid] = make_float4(nb.x, nb.y, nb.z, 0.f);
                 if (p.sig) p.sig[pid] = sig;
-                want_next = bounce < f.max_depth && max3(beta) > 0.0f;
+                want_next = cont;
                 if (want_next) {
-                    // plugin.mm:111-125 in double-float: phi = 2 pi r3, cos = sqrt(1 - r4), sin = sqrt(r4).
-                    ff sphi, cphi;
-                    ff_sincospi(2.0f * r3, sphi, cphi);
-                    const ff cos_t = ff_sqrt(two_sum(1.0f, -r4));
-                    const ff sin_t = ff_sqrt(ffv(r4));
-                    // v = normalize(cross(w, a)), a = (0,1,0) if |w.x| > 0.9 else (1,0,0)
-                    ff3 vv = fabsf(nrm.x.hi) > 0.9f ? ff3{ff_neg(nrm.z), ffv(0.0f), nrm.x}
-                                                    : ff3{ffv(0.0f), nrm.z, ff_neg(nrm.y)};
-                    vv = ff3_normalize(vv);
-                    const ff3 uu = ff3_cross(nrm, vv);
-                    const ff3 dir = ff3_normalize(ff3_add(ff3_add(ff3_scale(uu, ff_mul(cphi, sin_t)),
-                                                                  ff3_scale(vv, ff_mul(sphi, sin_t))),
-                                                          ff3_scale(nrm, cos_t)));
-                    ff_ray_store(&p.ray_ff[3ull * pid], org, dir);
-                    norg = ff3_f(org);
-                    nd = ff3_f(dir);
+                    ff_ray_store(&p.ray_ff[3ull * pid], v.org, v.dir);
+                    norg = ff3_f(v.org);
+                    nd = ff3_f(v.dir);
                 }
             }
         }
         const int ps = warp_append(0xffffffffu, want_shadow, shadow_count);
         if (want_shadow) {
-            shadow_q[3 * ps] = make_float4(sorg.x, sorg.y, sorg.z, __int_as_float(pid));
-            shadow_q[3 * ps + 1] = make_float4(wi_f.x, wi_f.y, wi_f.z, tmax_s);
+            shadow_q[3 * ps] = make_float4(v.so.x, v.so.y, v.so.z, __int_as_float(pid));
+            shadow_q[3 * ps + 1] = make_float4(v.sd.x, v.sd.y, v.sd.z, v.stmax);
             shadow_q[3 * ps + 2] = make_float4(contrib.x, contrib.y, contrib.z, 0.f);
         }
         const int pn = warp_append(0xffffffffu, want_next, next_count);
