@@ -107,16 +107,16 @@ def cpu_sample(scene, precision: int = 32, target_s: float = 12.0, seed: int = 0
 
     threads = threads or orc.hardware_threads()
     rng = np.random.default_rng(seed)
-    calib = rng.choice(WIDTH * HEIGHT, size=64, replace=False).astype(np.uint32)
-    t0 = time.perf_counter()
-    orc.render_nee(scene, WIDTH, HEIGHT, 4, DEPTH, seed=seed, precision=precision, threads=threads, pixels=calib)
-    build_and_calib = time.perf_counter() - t0
-    # one oracle call rebuilds its LBVH; time it separately on a 1-pixel render
+    # one oracle call rebuilds its LBVH; time that on a 1-pixel render and subtract it
+    calib = rng.choice(WIDTH * HEIGHT, size=4096, replace=False).astype(np.uint32)
     t0 = time.perf_counter()
     orc.render_nee(scene, WIDTH, HEIGHT, 1, 1, seed=seed, precision=precision, threads=threads, pixels=calib[:1])
     build_s = time.perf_counter() - t0
-    per_pixel_4spp = max(build_and_calib - build_s, 1e-3) / calib.size
-    npix = int(min(WIDTH * HEIGHT, max(64, target_s / (per_pixel_4spp * SPP / 4))))
+    # calibration: 4096 pixels at full spp, then size the timed sample to target_s
+    t0 = time.perf_counter()
+    orc.render_nee(scene, WIDTH, HEIGHT, SPP, DEPTH, seed=seed, precision=precision, threads=threads, pixels=calib)
+    per_pixel = max(time.perf_counter() - t0 - build_s, 1e-3) / calib.size
+    npix = int(min(WIDTH * HEIGHT, max(1024, target_s / per_pixel)))
     pix = rng.choice(WIDTH * HEIGHT, size=npix, replace=False).astype(np.uint32)
     t0 = time.perf_counter()
     out = orc.render_nee(scene, WIDTH, HEIGHT, SPP, DEPTH, seed=seed, precision=precision, threads=threads,
@@ -126,6 +126,191 @@ def cpu_sample(scene, precision: int = 32, target_s: float = 12.0, seed: int = 0
     desc = (f"{npix} random pixels of the 1920x1080 frame x 64 spp, depth 8 (soup-1M), FP{precision} oracle on "
             f"{threads} threads; {rays} rays in {dt:.2f} s (LBVH build {build_s:.2f} s excluded)")
     return rays / dt / 1e6, threads, desc
+
+
+def batch_scene_list(lib, count: int, seed0: int, tris: tuple[float, float], sizes: tuple[int, ...],
+                     spps: tuple[int, ...]) -> list:
+    """Soup scenes with seeds seed0 .. seed0 + count - 1; each scene's triangle count
+    (log-uniform in `tris`), square resolution and spp are drawn from numpy's default_rng
+    seeded with the scene seed."""
+    import math
+
+    import numpy as np
+
+    import quasi_gb300 as q
+
+    out = []
+    for i in range(count):
+        seed = seed0 + i
+        rng = np.random.default_rng(seed)
+        n = int(round(math.exp(rng.uniform(math.log(tris[0]), math.log(tris[1])))))
+        res = int(rng.choice(sizes))
+        spp = int(rng.choice(spps))
+        out.append((q.make_scene(f"soup:n={n},seed={seed}", lib), res, res, spp))
+    return out
+
+
+def bench_batch(host, stream, flush, steps: int, warmup: int, budget_ms: float) -> dict:
+    """Batching workload: 64 soup scenes (seeds 1..64, 1e3..5e5 triangles, 64^2..1024^2 pixels,
+    4/16/64 spp, depth 6) rendered as one batch (one graph launch per frame, autotuned),
+    against the same frames as 64 plain plugin renders, one scene after the other."""
+    import torch
+
+    import quasi_gb300 as q
+
+    scenes = batch_scene_list(host.lib, 64, 1, (1e3, 5e5), (64, 128, 256, 512, 1024), (4, 16, 64))
+    depth = 6
+    res = {"workload": "64 soup scenes, seeds 1..64, log-uniform 1e3..5e5 triangles, 64^2..1024^2 pixels, "
+                       "spp 4/16/64, depth 6, BVHs built once",
+           "tri_total": sum(s.tri_count for s, *_ in scenes),
+           "px_total": sum(w * h for _, w, h, _ in scenes),
+           "samples_per_frame": sum(w * h * spp for _, w, h, spp in scenes)}
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    h = stream.cuda_stream
+    with q.Batch(host, scenes, max_depth=depth) as b:
+        t0 = time.perf_counter()
+        chosen = b.autotune(budget_ms)
+        res["autotune_s"] = time.perf_counter() - t0
+        res["autotuned"] = {"form": ["wavefront", "megakernel"][chosen.form], "wave_paths": chosen.wave_paths,
+                            "trace_block": chosen.trace_block, "fetch_rays": chosen.fetch_rays}
+        for _ in range(warmup):
+            b.render(h)
+        b.synchronize()
+        st0 = b.stats()
+        ev0.record(stream)
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            b.render(h)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        st1 = b.stats()
+        ms = ev0.elapsed_time(ev1) / steps
+        rays = (st1.rays - st0.rays) / steps
+        res.update(value=rays / ms / 1e3, unit="Mrays/s", ms_per_frame=ms, rays_per_frame=rays, waves=st1.waves,
+                   kernels_per_frame=st1.kernels_per_frame, error_flags=st1.error_flags)
+    # the same frames as 64 plain renders (LBVH built once per scene, as in the batch)
+    hosts = []
+    try:
+        for sc, w, hh, spp in scenes:
+            ph = q.PluginHost(device=torch.cuda.current_device(), stream=h, width=w, height=hh)
+            ph.set_scene(sc)
+            ph.set_options(spp_per_frame=spp, max_depth=depth, seed=0, rebuild_each_frame=0)
+            hosts.append(ph)
+        for _ in range(warmup):
+            for ph in hosts:
+                ph.render(dirty=False, stream=h)
+        torch.cuda.synchronize()
+        r0 = sum(ph.stats().total_rays for ph in hosts)
+        ev0.record(stream)
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            for ph in hosts:
+                ph.render(dirty=False, stream=h)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        r1 = sum(ph.stats().total_rays for ph in hosts)
+        pms = ev0.elapsed_time(ev1) / steps
+        prays = (r1 - r0) / steps
+        res.update(plain_value=prays / pms / 1e3, plain_ms_per_frame=pms, plain_rays_per_frame=prays,
+                   speedup=(rays / ms) / (prays / pms) if prays else None)
+    finally:
+        for ph in hosts:
+            ph.destroy()
+    return res
+
+
+def bench_diff(stream, steps: int, fit_steps: int) -> dict:
+    """Differentiation workloads: (a) forward vs adjoint cost on the 10,000-triangle soup
+    (seed 7), 512x512, 16 spp, depth 4; (b) 32 soup scenes (seeds 101..132, 2e3..1e5
+    triangles, 128^2..512^2 pixels, 8 spp, depth 4) fitted by Adam (lr 0.01) from albedo
+    perturbed by N(0, 0.1) clamped to [0.05, 0.95], one forward and one adjoint graph launch
+    per step."""
+    import numpy as np
+    import torch
+
+    import quasi_gb300 as q
+    from quasi_gb300 import autograd as qa
+
+    out = {}
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    with torch.cuda.stream(stream):
+        # (a) adjoint cost
+        scene = q.make_scene("soup:n=10000,seed=7")
+        w = hh = 512
+        spp = 16
+        host = qa.make_host(scene, w, hh, max_depth=4, seed=0)
+        alb = torch.tensor(scene.albedo, device="cuda", requires_grad=True)
+        emi = torch.tensor(scene.emission, device="cuda", requires_grad=True)
+        rng = np.random.default_rng(7)
+        tgt_alb = np.clip(scene.albedo + rng.normal(0.0, 0.1, scene.albedo.shape), 0.05, 0.95).astype(np.float32)
+        with torch.no_grad():
+            target = qa.render(torch.tensor(tgt_alb, device="cuda"), emi.detach(), host, w, hh, spp).clone()
+        fwd_ms, bwd_ms = [], []
+        r_f = r_b = 0
+        for i in range(2 + steps):
+            s0 = host.stats()
+            ev[0].record()
+            img = qa.render(alb, emi, host, w, hh, spp)
+            loss = ((img - target) ** 2).sum()
+            ev[1].record()
+            loss.backward()
+            ev[2].record()
+            torch.cuda.synchronize()
+            s1 = host.stats()
+            alb.grad = None
+            emi.grad = None
+            if i >= 2:
+                fwd_ms.append(ev[0].elapsed_time(ev[1]))
+                bwd_ms.append(ev[1].elapsed_time(ev[2]))
+                r_f += s1.total_rays - s0.total_rays
+                r_b += s1.adjoint_rays - s0.adjoint_rays
+        host.destroy()
+        f, bk = sum(fwd_ms), sum(bwd_ms)
+        out["adjoint"] = {"workload": "soup-10k seed 7, 512x512, 16 spp, depth 4, L2 loss",
+                          "forward_ms": f / steps, "adjoint_ms": bk / steps, "adjoint_over_forward": bk / f,
+                          "forward_mrays_s": r_f / f / 1e3, "adjoint_mrays_s": r_b / bk / 1e3,
+                          "rays_forward": r_f / steps, "rays_adjoint": r_b / steps}
+        # (b) batched differentiation
+        lib = q.load_library()
+        scenes = batch_scene_list(lib, 32, 101, (2e3, 1e5), (128, 256, 512), (8,))
+        bhost, batch = qa.make_batch(scenes, max_depth=4, seed=0)
+        gt = torch.tensor(np.concatenate([sc.albedo for sc, *_ in scenes]), device="cuda")
+        em = torch.tensor(np.concatenate([sc.emission for sc, *_ in scenes]), device="cuda")
+        rng = np.random.default_rng(2024)
+        init = torch.tensor(np.clip(gt.cpu().numpy() + rng.normal(0.0, 0.1, gt.shape), 0.05, 0.95).astype(np.float32),
+                            device="cuda")
+        with torch.no_grad():
+            target = qa.render_batch(gt, em, batch).clone()
+        # triangles the images depend on: nonzero albedo gradient at the start
+        a0 = init.clone().requires_grad_(True)
+        ((qa.render_batch(a0, em, batch) - target) ** 2).mean().backward()
+        seen = (a0.grad.abs().sum(dim=1) > 0)
+        st0 = batch.stats()
+        ev[0].record()
+        fitted, losses = qa.fit_albedo(batch, target, init, em, steps=fit_steps, lr=0.01)
+        ev[1].record()
+        torch.cuda.synchronize()
+        st1 = batch.stats()
+        ms = ev[0].elapsed_time(ev[1])
+        rays = (st1.rays - st0.rays) + (st1.adjoint_rays - st0.adjoint_rays)
+
+        def rmse(a, m=None):
+            d = (a - gt) if m is None else (a - gt)[m]
+            return float(torch.sqrt((d ** 2).mean()))
+
+        out["batched_fit"] = {
+            "workload": "32 soup scenes, seeds 101..132, log-uniform 2e3..1e5 triangles, 128^2..512^2 pixels, "
+                        "8 spp, depth 4, Adam lr 0.01",
+            "steps": fit_steps, "tri_total": int(gt.shape[0]), "px_total": int(st1.px_total),
+            "mrays_s_forward_plus_adjoint": rays / ms / 1e3, "ms_per_step": ms / fit_steps,
+            "rmse_init_all": rmse(init), "rmse_final_all": rmse(fitted),
+            "triangles_seen": int(seen.sum()), "rmse_init_seen": rmse(init, seen), "rmse_final_seen": rmse(fitted, seen),
+            "loss_first": losses[0], "loss_last": losses[-1], "graph_launches_per_step": 2}
+        batch.destroy()
+        bhost.destroy()
+    return out
 
 
 def run_reference(args) -> None:
@@ -268,6 +453,12 @@ def run_ours(args) -> None:
                 "avg_launch_ms": kms / n_launch, "launches": n_launch, "kernel_share": share,
                 "bytes_model": "closest: rays*(32+16) + node_visits*64 + tri_tests*48; shadow: rays*48 + node_visits*64 + tri_tests*48 (counted in an untimed frame)"}
 
+    batch = diff = None
+    if rank == 0 and not args.no_batch:
+        batch = bench_batch(host, stream, flush, steps=2, warmup=1, budget_ms=args.tune_ms)
+    if rank == 0 and not args.no_diff:
+        diff = bench_diff(stream, steps=3, fit_steps=args.fit_steps)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         v, cores, desc = cpu_sample(scene, precision=32, target_s=args.ref_seconds)
@@ -283,7 +474,7 @@ def run_ours(args) -> None:
                            "timed region)", "parallelism": f"replicas x{world}", "wave_spp": args.wave_spp,
                            "trace_block": args.trace_block},
                 "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
-                "clocks": clocks.summary()}
+                "clocks": clocks.summary(), "batch": batch, "diff": diff}
         print(json.dumps(line), flush=True)
     host.destroy()
     if world > 1:
@@ -301,6 +492,10 @@ def main() -> None:
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-scene batching workload")
+    ap.add_argument("--no-diff", action="store_true", help="skip the differentiation workloads")
+    ap.add_argument("--tune-ms", type=float, default=5000.0, help="batch autotuner budget")
+    ap.add_argument("--fit-steps", type=int, default=100, help="Adam steps of the batched fit")
     # Size overrides, for profiling captures on a small case only (not benchmark numbers).
     ap.add_argument("--width", type=int, default=WIDTH)
     ap.add_argument("--height", type=int, default=HEIGHT)

@@ -193,7 +193,7 @@ typedef struct Q_cuda_options {
     uint32_t profile;            /* time every kernel launch with CUDA events */
     uint32_t megakernel;         /* 1 = one-kernel path tracer instead of the wavefront */
     uint32_t smem_levels;        /* top BVH levels staged in shared memory per block
-                                    (0 = default 7, 1..9, 32 = none) */
+                                    (0 = default 5, 1..9, 32 = none) */
     float ray_eps;               /* ray origin offset along the normal (1e-4) */
     uint32_t refill_lanes;       /* trace kernels refill a warp once this many lanes idle
                                     (1..32; 32 = refill only whole warps; 0 = default) */
@@ -215,6 +215,7 @@ typedef struct Q_cuda_stats {
     uint32_t error_flags;     /* device-side error bits (QUASI_DEVERR_*) */
     double frame_ms;          /* device time of the last frame (events on the stream) */
     double bvh_ms;            /* device time of the last LBVH build */
+    uint64_t adjoint_rays;    /* rays replayed by Q_cuda_backward since the plugin was created */
 } Q_cuda_stats;
 
 #define QUASI_DEVERR_STACK     1u
@@ -316,9 +317,105 @@ Q_CUDA_EXPORT int Q_cuda_backward(Q_plugin_handle* handle, const float* device_g
                                   uint32_t sample_base, float* device_grad_albedo,
                                   float* device_grad_emission, void* stream);
 
-/* Runs the autotuner on the current scene/options and stores the result in the options
- * (wave_spp, trace_block). budget_ms bounds the time spent. */
+/* Runs the autotuner on the current scene, frame size and options: times short frames
+ * (at most 8 spp) of each candidate form (wavefront or megakernel), wave size, trace block
+ * size and shared-memory treelet depth, keeps the fastest in the options (megakernel,
+ * wave_spp, trace_block, smem_levels) and resets the accumulation. Needs a previous render
+ * (for the frame size). budget_ms bounds the time spent (0 = 2000 ms). */
 Q_CUDA_EXPORT int Q_cuda_autotune(Q_plugin_handle* handle, double budget_ms);
+
+/* ------------------------------------------------------------- Part 3: scene batches
+ *
+ * Many scenes of uneven size rendered together (no reference counterpart): every frame
+ * renders spp samples of every pixel of every scene as one launch sequence over all of
+ * them, fed from a device table of work items (runs of whole sample planes, packed into
+ * waves of wave_paths path slots), captured once as a CUDA graph and replayed. Each
+ * scene's image is bit-identical to rendering that scene alone through the plugin with the
+ * same seed, depth and ray_eps. A batch belongs to the plugin handle it was created from
+ * (same device, stream by default) and must be destroyed before that handle. */
+typedef struct Q_cuda_batch Q_cuda_batch;
+
+typedef struct Q_cuda_batch_scene {
+    const Q_cuda_scene* scene; /* triangles, materials and camera (quads are ignored) */
+    uint32_t width;
+    uint32_t height;
+    uint32_t spp;              /* samples per pixel per Q_cuda_batch_render */
+} Q_cuda_batch_scene;
+
+#define QUASI_BATCH_WAVEFRONT  0u
+#define QUASI_BATCH_MEGAKERNEL 1u
+
+/* Zero-initialise and set what you need; a zero field means default. */
+typedef struct Q_cuda_batch_options {
+    uint32_t max_depth;     /* path vertices after the camera (6) */
+    uint32_t seed;          /* RNG seed, shared by all scenes (0) */
+    uint32_t form;          /* QUASI_BATCH_WAVEFRONT (default) or QUASI_BATCH_MEGAKERNEL */
+    uint32_t wave_paths;    /* path slots per wave (0 = 8M; raised to the largest sample plane) */
+    uint32_t trace_block;   /* threads per block of the persistent kernels (0 = 128) */
+    uint32_t fetch_rays;    /* rays or paths a warp takes per atomic, multiple of 32 (0 = 32) */
+    uint32_t use_graph;     /* 0 = default (graph), 1 = graph, 2 = plain launches */
+    uint32_t collect_stats; /* count BVH node visits and triangle tests */
+    float ray_eps;          /* ray origin offset along the normal (1e-4) */
+} Q_cuda_batch_options;
+
+typedef struct Q_cuda_batch_stats {
+    uint64_t frames;            /* frames rendered since the last reset */
+    uint64_t camera_rays;       /* per frame (fixed by the batch) */
+    uint64_t closest_rays;      /* closest-hit rays (camera rays included), since the last reset */
+    uint64_t shadow_rays;       /* since the last reset */
+    uint64_t node_visits;       /* with collect_stats, since the last reset */
+    uint64_t tri_tests;         /* with collect_stats, since the last reset */
+    uint32_t scenes;
+    uint32_t waves;             /* waves per frame */
+    uint32_t kernels_per_frame; /* kernel launches (graph kernel nodes) per frame */
+    uint32_t error_flags;       /* QUASI_DEVERR_* bits */
+    uint64_t tri_total;         /* triangles of all scenes */
+    uint64_t px_total;          /* pixels of all scenes (the batch image pool) */
+    double frame_ms;            /* device time of the last frame */
+    uint64_t adjoint_rays;      /* rays replayed by Q_cuda_batch_backward since the last reset */
+} Q_cuda_batch_stats;
+
+/* Uploads the scenes and builds their LBVHs. *out receives the batch; on failure returns
+ * an error (details in Q_cuda_last_error(handle)). */
+Q_CUDA_EXPORT int Q_cuda_batch_create(Q_plugin_handle* handle, const Q_cuda_batch_scene* scenes, uint32_t count,
+                                      const Q_cuda_batch_options* options, Q_cuda_batch** out);
+Q_CUDA_EXPORT void Q_cuda_batch_destroy(Q_cuda_batch* batch);
+/* Changes options (the next frame re-plans and re-captures); resets the accumulation. */
+Q_CUDA_EXPORT int Q_cuda_batch_set_options(Q_cuda_batch* batch, const Q_cuda_batch_options* options);
+Q_CUDA_EXPORT int Q_cuda_batch_get_options(Q_cuda_batch* batch, Q_cuda_batch_options* options);
+/* Renders one frame of every scene on `stream` (NULL = the plugin's stream; (void*)1 =
+ * cudaStreamLegacy); asynchronous. */
+Q_CUDA_EXPORT int Q_cuda_batch_render(Q_cuda_batch* batch, void* stream);
+/* Clears the accumulation of every scene (the next frame starts at sample 0). */
+Q_CUDA_EXPORT int Q_cuda_batch_reset(Q_cuda_batch* batch);
+/* Waits for the batch's work; returns QUASI_ERR_STACK / QUASI_ERR_TIMEOUT for device errors. */
+Q_CUDA_EXPORT int Q_cuda_batch_synchronize(Q_cuda_batch* batch);
+Q_CUDA_EXPORT int Q_cuda_batch_get_stats(Q_cuda_batch* batch, Q_cuda_batch_stats* stats);
+/* Mean HDR image of scene `index` as host RGBA float (width*height*4, top row first). */
+Q_CUDA_EXPORT int Q_cuda_batch_readback(Q_cuda_batch* batch, uint32_t index, float* host_rgba);
+/* Mean HDR images of all scenes as device RGB float: scene after scene, 3 floats per pixel,
+ * px_total pixels (the layout of the gradient image of Q_cuda_batch_backward). */
+Q_CUDA_EXPORT int Q_cuda_batch_resolve_device(Q_cuda_batch* batch, float* device_rgb, void* stream);
+/* Triangle and pixel offsets of scene `index` in the batch pools (either may be NULL). */
+Q_CUDA_EXPORT int Q_cuda_batch_offsets(Q_cuda_batch* batch, uint32_t index, uint64_t* tri_offset,
+                                       uint64_t* px_offset);
+/* Replaces the materials of all scenes from DEVICE arrays (tri_total*3 floats each, scenes
+ * back to back; either may be NULL to keep it) and resets the accumulation. */
+Q_CUDA_EXPORT int Q_cuda_batch_set_materials_device(Q_cuda_batch* batch, const float* device_albedo,
+                                                    const float* device_emission, void* stream);
+/* Path-replay adjoint of the last frame of every scene: device_grad_image holds
+ * dLoss/dI for every pixel of the batch image pool (layout of Q_cuda_batch_resolve_device);
+ * gradients are written (not accumulated) to tri_total*3 floats each. Captured as a CUDA
+ * graph like the frame. */
+Q_CUDA_EXPORT int Q_cuda_batch_backward(Q_cuda_batch* batch, const float* device_grad_image,
+                                        float* device_grad_albedo, float* device_grad_emission, void* stream);
+/* Times short frames (at most tune_spp = 1 sample per pixel of every scene) of each
+ * candidate form, wave size, block size and fetch size, keeps the fastest in the options,
+ * writes them to *chosen (may be NULL) and resets the accumulation. budget_ms bounds the
+ * time spent (0 = 5000 ms). */
+Q_CUDA_EXPORT int Q_cuda_batch_autotune(Q_cuda_batch* batch, double budget_ms, Q_cuda_batch_options* chosen);
+/* Message of the batch's last failed call (owned by the batch). */
+Q_CUDA_EXPORT const char* Q_cuda_batch_last_error(Q_cuda_batch* batch);
 
 #ifdef __cplusplus
 } /* extern "C" */

@@ -22,12 +22,17 @@ QUASI_ERR_OOM = -3
 QUASI_ERR_TIMEOUT = -4
 QUASI_ERR_STACK = -5
 QUASI_ERR_STATE = -6
+QUASI_ERR_TOO_LARGE = -7
 
 QUASI_INTEGRATOR_NEE = 0
 QUASI_INTEGRATOR_REFERENCE = 1
 
 QUASI_DEVERR_STACK = 1
 QUASI_DEVERR_TIMEOUT = 2
+QUASI_DEVERR_TRAVERSAL = 4
+
+QUASI_BATCH_WAVEFRONT = 0
+QUASI_BATCH_MEGAKERNEL = 1
 
 
 class Q_gpu_context(C.Structure):
@@ -95,7 +100,7 @@ class Q_cuda_stats(C.Structure):
                 ("node_visits", C.c_uint64), ("tri_tests", C.c_uint64), ("shadow_node_visits", C.c_uint64),
                 ("shadow_tri_tests", C.c_uint64), ("total_rays", C.c_uint64), ("samples_accumulated", C.c_uint64),
                 ("kernel_launches", C.c_uint32), ("error_flags", C.c_uint32), ("frame_ms", C.c_double),
-                ("bvh_ms", C.c_double)]
+                ("bvh_ms", C.c_double), ("adjoint_rays", C.c_uint64)]
 
     @property
     def rays(self) -> int:
@@ -104,6 +109,30 @@ class Q_cuda_stats(C.Structure):
 
 class Q_cuda_kernel_time(C.Structure):
     _fields_ = [("name", C.c_char * 48), ("launches", C.c_uint32), ("total_ms", C.c_double)]
+
+
+class Q_cuda_batch_scene(C.Structure):
+    _fields_ = [("scene", C.POINTER(Q_cuda_scene)), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("spp", C.c_uint32)]
+
+
+class Q_cuda_batch_options(C.Structure):
+    _fields_ = [("max_depth", C.c_uint32), ("seed", C.c_uint32), ("form", C.c_uint32), ("wave_paths", C.c_uint32),
+                ("trace_block", C.c_uint32), ("fetch_rays", C.c_uint32), ("use_graph", C.c_uint32),
+                ("collect_stats", C.c_uint32), ("ray_eps", C.c_float)]
+
+
+class Q_cuda_batch_stats(C.Structure):
+    _fields_ = [("frames", C.c_uint64), ("camera_rays", C.c_uint64), ("closest_rays", C.c_uint64),
+                ("shadow_rays", C.c_uint64), ("node_visits", C.c_uint64), ("tri_tests", C.c_uint64),
+                ("scenes", C.c_uint32), ("waves", C.c_uint32), ("kernels_per_frame", C.c_uint32),
+                ("error_flags", C.c_uint32), ("tri_total", C.c_uint64), ("px_total", C.c_uint64),
+                ("frame_ms", C.c_double), ("adjoint_rays", C.c_uint64)]
+
+    @property
+    def rays(self) -> int:
+        """Rays traced since the last reset (closest-hit, camera included, plus shadow)."""
+        return self.closest_rays + self.shadow_rays
 
 
 # Symbol table: name -> (restype, argtypes). Required/optional split follows
@@ -145,4 +174,20 @@ CUDA_SYMBOLS = {
     "Q_cuda_set_materials_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32]),
     "Q_cuda_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
                                   C.c_void_p]),
+    "Q_cuda_batch_create": (C.c_int, [C.c_void_p, C.POINTER(Q_cuda_batch_scene), C.c_uint32,
+                                      C.POINTER(Q_cuda_batch_options), C.POINTER(C.c_void_p)]),
+    "Q_cuda_batch_destroy": (None, [C.c_void_p]),
+    "Q_cuda_batch_set_options": (C.c_int, [C.c_void_p, C.POINTER(Q_cuda_batch_options)]),
+    "Q_cuda_batch_get_options": (C.c_int, [C.c_void_p, C.POINTER(Q_cuda_batch_options)]),
+    "Q_cuda_batch_render": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "Q_cuda_batch_reset": (C.c_int, [C.c_void_p]),
+    "Q_cuda_batch_synchronize": (C.c_int, [C.c_void_p]),
+    "Q_cuda_batch_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Q_cuda_batch_stats)]),
+    "Q_cuda_batch_readback": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),
+    "Q_cuda_batch_resolve_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "Q_cuda_batch_offsets": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "Q_cuda_batch_set_materials_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "Q_cuda_batch_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "Q_cuda_batch_autotune": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(Q_cuda_batch_options)]),
+    "Q_cuda_batch_last_error": (C.c_char_p, [C.c_void_p]),
 }

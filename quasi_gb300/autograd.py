@@ -5,6 +5,10 @@ renders `spp` samples per pixel through the plugin and resolves the mean HDR ima
 torch tensor. Backward calls the path-replay adjoint (Q_cuda_backward), which regenerates
 the same paths from their RNG keys and returns dLoss/dalbedo and dLoss/demission.
 
+render_batch does the same for a scene batch (Q_cuda_batch_*): one captured graph renders
+every scene, one captured graph runs the adjoint of every scene; materials and images are
+the batch pools (scenes back to back). fit_albedo drives Adam with it.
+
 Every plugin call is issued on torch's current CUDA stream, so the tensors it reads and
 writes are ordered with the surrounding torch work without extra synchronisation. torch's
 default stream has the handle 0, which the plugin ABI reads as "use your own stream"; it is
@@ -16,7 +20,7 @@ import ctypes as C
 
 import torch
 
-from .host import PluginHost, QuasiError
+from .host import Batch, PluginHost, QuasiError
 
 CUDA_STREAM_LEGACY = 1
 
@@ -76,3 +80,63 @@ def render(albedo: torch.Tensor, emission: torch.Tensor, host: PluginHost, width
            sample_base: int = 0) -> torch.Tensor:
     """Differentiable render: returns the (height, width, 3) mean image of `spp` samples."""
     return RenderFunction.apply(albedo, emission, host, width, height, spp, sample_base)
+
+
+class BatchRenderFunction(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, albedo: torch.Tensor, emission: torch.Tensor, batch: Batch, px_total: int):
+        if not (albedo.is_cuda and emission.is_cuda):
+            raise ValueError("albedo and emission must be CUDA tensors")
+        a = albedo.detach().float().contiguous()
+        e = emission.detach().float().contiguous()
+        stream = torch_stream_handle()
+        batch.set_materials_device(a.data_ptr(), e.data_ptr(), stream)
+        batch.render(stream)
+        out = torch.empty((px_total, 3), dtype=torch.float32, device=albedo.device)
+        batch.resolve_device(out.data_ptr(), stream)
+        ctx.batch, ctx.n = batch, a.shape[0]
+        ctx.keep = (a, e)
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_image: torch.Tensor):
+        g = grad_image.detach().float().contiguous()
+        ga = torch.empty((ctx.n, 3), dtype=torch.float32, device=g.device)
+        ge = torch.empty((ctx.n, 3), dtype=torch.float32, device=g.device)
+        ctx.batch.backward(g.data_ptr(), ga.data_ptr(), ge.data_ptr(), torch_stream_handle())
+        return ga, ge, None, None
+
+
+def make_batch(scenes, max_depth: int = 4, seed: int = 0, **options) -> tuple[PluginHost, Batch]:
+    """A plugin instance on torch's current stream and a batch of `scenes`
+    [(Scene, width, height, spp), ...]."""
+    host = PluginHost(stream=torch_stream_handle())
+    batch = Batch(host, scenes, max_depth=max_depth, seed=seed, **options)
+    return host, batch
+
+
+def render_batch(albedo: torch.Tensor, emission: torch.Tensor, batch: Batch) -> torch.Tensor:
+    """Differentiable render of every scene: returns the (px_total, 3) pool of mean images
+    (scene after scene, rows top first); albedo/emission are (tri_total, 3)."""
+    return BatchRenderFunction.apply(albedo, emission, batch, int(batch.stats().px_total))
+
+
+def fit_albedo(batch: Batch, target: torch.Tensor, albedo0: torch.Tensor, emission: torch.Tensor, steps: int = 100,
+               lr: float = 0.01) -> tuple[torch.Tensor, list[float]]:
+    """Adam on the per-triangle albedo of every scene of the batch against target images
+    (L2 loss, mean over pixels and channels); albedo is kept in [0, 1] after each step.
+    Returns the fitted albedo and the loss of every step."""
+    albedo = albedo0.detach().clone().requires_grad_(True)
+    opt = torch.optim.Adam([albedo], lr=lr)
+    px = int(batch.stats().px_total)
+    losses = []
+    for _ in range(steps):
+        opt.zero_grad(set_to_none=True)
+        img = BatchRenderFunction.apply(albedo, emission, batch, px)
+        loss = ((img - target) ** 2).mean()
+        loss.backward()
+        opt.step()
+        with torch.no_grad():
+            albedo.clamp_(0.0, 1.0)
+        losses.append(loss.detach())
+    return albedo.detach(), [float(v) for v in losses]

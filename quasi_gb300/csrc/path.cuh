@@ -1,0 +1,427 @@
+// path.cuh - per-path device code shared by every form of the NEE path tracer: the
+// single-scene wavefront (wavefront_kernels.cuh), the one-thread-per-path megakernel and
+// adjoint (megakernel.cuh) and the multi-scene batch (batch_kernels.cuh).
+//
+// A path is addressed by its scene-local id `local` = j * slots + slot: sample
+// f.sample_base + j of the pixel at `slot` (pixel slots are ordered in 8x4 tiles). Its state
+// lives at a path-state index `pid` of the current wave's buffers; the single-scene renderer
+// uses pid == local (per wave), the batch maps pid -> (scene, local) through a table.
+// Every form calls the same functions here with the same keys, so a path sample gets the
+// same radiance bit for bit whichever form traced it.
+#pragma once
+
+#include "common.cuh"
+#include "ffmath.cuh"
+#include "shading.cuh"
+#include "trace.cuh"
+
+namespace quasi {
+
+// Camera basis (plugin.mm:134-147) as double-float vectors, split on the host from double.
+struct CameraFF {
+    float3 origin;
+    float3 ll_hi, ll_lo, h_hi, h_lo, v_hi, v_lo;
+};
+
+struct FrameParams {
+    CameraFF cam;
+    uint32_t width, height, tiles_x, slots;
+    uint32_t wave_spp, sample_base;
+    uint32_t seed, max_depth;
+    float eps;
+    uint32_t frame_spp, wave_offset;
+};
+
+struct SceneDev {
+    const float4* tri_in;   // original order, v0 v1 v2
+    const float4* albedo;
+    const float4* emission;
+    const int* emitters;
+    const float4* nodes;
+    const float4* tris;     // leaf order, v0+orig, e1, e2
+    uint32_t n_tris, n_emit;
+    int refill;             // idle lanes that trigger a ray refill in the trace kernels
+    int steps;              // node visits per lane between refill checks
+    const float4* tree;     // top BVH levels, breadth first, staged in shared memory
+    int tree_n;             // nodes in `tree` (0 = no staging)
+};
+
+// Copies the treelet into the block's shared memory (dynamic size tree_n * 64 bytes).
+__device__ __forceinline__ const float4* stage_treelet(const SceneDev& s) {
+    extern __shared__ float4 s_tree[];
+    for (int i = threadIdx.x; i < 4 * s.tree_n; i += blockDim.x) s_tree[i] = __ldg(&s.tree[i]);
+    __syncthreads();
+    return s_tree;
+}
+
+struct PathDev {
+    float4* beta;
+    float4* lpath;
+    float4* aov_a;   // first-hit albedo (rgb) + depth (w)
+    float4* aov_n;   // first-hit remapped normal
+    float4* ray_ff;  // 3 float4 per path: the double-float ray of the path's next segment
+    uint32_t* sig;   // path signatures (record mode) or null
+};
+
+// Pixel slots are ordered in 8x4 tiles so a warp's camera rays cover a compact patch.
+__device__ __forceinline__ void slot_to_xy(uint32_t slot, uint32_t tiles_x, uint32_t& x, uint32_t& y) {
+    const uint32_t tile = slot >> 5, in = slot & 31u;
+    const uint32_t ty = tile / tiles_x, tx = tile - ty * tiles_x;
+    x = tx * 8u + (in & 7u);
+    y = ty * 4u + (in >> 3);
+}
+__device__ __forceinline__ uint32_t xy_to_slot(uint32_t x, uint32_t y, uint32_t tiles_x) {
+    return ((((y >> 2) * tiles_x) + (x >> 3)) << 5) | ((y & 3u) << 3) | (x & 7u);
+}
+
+__device__ __forceinline__ void kahan_add(float& sum, float& comp, float x) {
+    const float y = x - comp;
+    const float t = sum + y;
+    comp = (t - sum) - y;
+    sum = t;
+}
+
+__device__ __forceinline__ ff3 ff3_pair(float3 hi, float3 lo) {
+    return ff3{ff{hi.x, lo.x}, ff{hi.y, lo.y}, ff{hi.z, lo.z}};
+}
+
+template <bool STATS>
+__device__ __forceinline__ void flush_counters(const TraceCounters& c, unsigned long long* stats) {
+    if (!STATS) return;
+    uint32_t a = c.nodes, b = c.tris;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&stats[0], static_cast<unsigned long long>(a));
+        atomicAdd(&stats[1], static_cast<unsigned long long>(b));
+    }
+}
+
+// Adds a per-thread count to *out with one atomic per warp (all lanes must call).
+__device__ __forceinline__ void warp_add_count(int v, unsigned long long* out) {
+    unsigned long long x = static_cast<unsigned long long>(v);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0 && x) atomicAdd(out, x);
+}
+
+// Camera ray of (pixel x,y; sample) in double-float: jitter (r1, r2) inside the pixel,
+// u = (x + r1) / W, v = 1 - (y + r2) / H, direction = normalize(ll + u h + v v' - o).
+__device__ __forceinline__ void camera_ray_ff(const FrameParams& f, uint32_t x, uint32_t y, uint32_t sample, ff3& o,
+                                              ff3& d) {
+    uint32_t st = path_key(f.seed, y * f.width + x, sample, 0u);
+    const float jx = rng_next(st);
+    const float jy = rng_next(st);
+    const ff u = ff_div(two_sum(static_cast<float>(x), jx), ffv(static_cast<float>(f.width)));
+    const ff v = ff_sub(ffv(1.0f), ff_div(two_sum(static_cast<float>(y), jy), ffv(static_cast<float>(f.height))));
+    d = ff3_normalize(ff3_sub(ff3_add(ff3_add(ff3_pair(f.cam.ll_hi, f.cam.ll_lo), ff3_scale(ff3_pair(f.cam.h_hi, f.cam.h_lo), u)),
+                                      ff3_scale(ff3_pair(f.cam.v_hi, f.cam.v_lo), v)),
+                              ff3v(f.cam.origin)));
+    o = ff3v(f.cam.origin);
+}
+
+// Starts path `local` in state slot `pid`: returns false for a slot outside the image;
+// otherwise initialises the state and returns the FP32 camera ray in (o, d).
+__device__ __forceinline__ bool begin_path(const FrameParams& f, const PathDev& p, uint32_t pid, uint32_t local,
+                                           float3& o, float3& d) {
+    const uint32_t j = local / f.slots;
+    uint32_t x, y;
+    slot_to_xy(local - j * f.slots, f.tiles_x, x, y);
+    if (x >= f.width || y >= f.height) return false;
+    ff3 ro, rd;
+    camera_ray_ff(f, x, y, f.sample_base + j, ro, rd);
+    ff_ray_store(&p.ray_ff[3ull * pid], ro, rd);
+    o = f.cam.origin;
+    d = ff3_f(rd);
+    p.beta[pid] = make_float4(1.f, 1.f, 1.f, 0.f);
+    p.lpath[pid] = make_float4(0.f, 0.f, 0.f, 0.f);
+    p.aov_a[pid] = make_float4(0.f, 0.f, 0.f, 0.f);
+    p.aov_n[pid] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (p.sig) p.sig[pid] = 0u;
+    return true;
+}
+
+// Closest-hit queue: ray i is q[2i] = (origin, path id), q[2i+1] = (direction, excluded
+// triangle); the result is hits[i] = (t, triangle or -1, u, v).
+struct ClosestJob {
+    const float4* __restrict__ q;
+    float4* __restrict__ hits;
+    __device__ __forceinline__ int pid(int i) const { return __float_as_int(q[2 * i].w); }
+    __device__ __forceinline__ void load(int i, float3& o, float3& d, float& tmax, int& exclude) const {
+        const float4 r0 = q[2 * i], r1 = q[2 * i + 1];
+        o = xyz(r0);
+        d = xyz(r1);
+        tmax = __int_as_float(0x7f800000);
+        exclude = __float_as_int(r1.w);
+    }
+    __device__ __forceinline__ void store(int i, const TraceState& s) const {
+        hits[i] = make_float4(s.best_t, __int_as_float(s.best), s.bu, s.bv);
+    }
+};
+
+// Shadow queue: sq[3i] = (origin, path id), sq[3i+1] = (direction, t_max), sq[3i+2] =
+// (contribution); an unoccluded ray adds its contribution to the path's radiance.
+struct ShadowJob {
+    const float4* __restrict__ sq;
+    PathDev p;
+    __device__ __forceinline__ int pid(int i) const { return __float_as_int(sq[3 * i].w); }
+    __device__ __forceinline__ void load(int i, float3& o, float3& d, float& tmax, int& exclude) const {
+        const float4 r0 = sq[3 * i], r1 = sq[3 * i + 1];
+        o = xyz(r0);
+        d = xyz(r1);
+        tmax = r1.w;
+        exclude = -1;
+    }
+    __device__ __forceinline__ void store(int i, const TraceState& s) const {
+        const int pid = __float_as_int(sq[3 * i].w);
+        if (s.best < 0) {
+            const float4 c = sq[3 * i + 2];
+            float4 L = p.lpath[pid];
+            L.x += c.x;
+            L.y += c.y;
+            L.z += c.z;
+            p.lpath[pid] = L;
+        }
+        if (p.sig) p.sig[pid] = sig_mix(p.sig[pid], s.best < 0 ? k_sig_lit : k_sig_shadowed);
+    }
+};
+
+// Traversal modes of the persistent trace kernels.
+constexpr int k_mode_batch = 0;       // warp batches of 32 rays, nodes from global memory
+constexpr int k_mode_batch_tree = 1;  // warp batches, top levels from shared memory
+constexpr int k_mode_refill = 2;      // per-lane refill (trace_persistent)
+
+// What shading one closest hit asks the wavefront to enqueue.
+struct HitShade {
+    bool shadow;            // enqueue the shadow ray (so, sd, stmax) carrying `contrib`
+    bool next;              // enqueue the continuation ray (norg, nd)
+    float3 contrib;
+    float3 so, sd;
+    float stmax;
+    float3 norg, nd;
+};
+
+// Shades the closest hit h = (t, prim >= 0, u, v) at bounce `bounce` of path `local` (state
+// slot `pid`): first-hit emission and AOVs, the NEE sample and the continuation direction.
+// Updates beta, the signature and the stored double-float ray of the path.
+__device__ __forceinline__ void shade_hit(const FrameParams& f, const SceneDev& s, const PathDev& p, uint32_t bounce,
+                                          int pid, uint32_t local, float4 h, HitShade& o) {
+    const VertexScene vs{s.tri_in, s.albedo, s.emission, s.emitters, s.n_emit, f.eps};
+    const int prim = __float_as_int(h.y);
+    ff3 ro, rd;
+    ff_ray_load(&p.ray_ff[3ull * pid], ro, rd);
+    const uint32_t j = local / f.slots;
+    uint32_t px, py;
+    slot_to_xy(local - j * f.slots, f.tiles_x, px, py);
+    const uint32_t key = path_key(f.seed, py * f.width + px, f.sample_base + j, bounce);
+    const float3 alb = xyz(__ldg(&s.albedo[prim]));
+    const float3 beta = xyz(p.beta[pid]);
+    const float3 nb = beta * alb;
+    const bool cont = bounce < f.max_depth && max3(nb) > 0.0f;
+    VertexResult v;
+    shade_vertex(vs, key, prim, h, ro, rd, cont, v);
+    uint32_t sig = p.sig ? sig_mix(p.sig[pid], static_cast<uint32_t>(prim)) : 0u;
+    if (bounce == 1) {
+        const float3 em = xyz(__ldg(&s.emission[prim]));
+        p.lpath[pid] = make_float4(em.x, em.y, em.z, 0.f);
+        first_hit_aovs(alb, em, h.x, v.nrm, p.aov_a[pid], p.aov_n[pid]);
+    }
+    o.shadow = v.nee;
+    if (v.nee) {
+        o.contrib = beta * alb * xyz(__ldg(&s.emission[v.light])) * v.g;
+        o.so = v.so;
+        o.sd = v.sd;
+        o.stmax = v.stmax;
+    } else {
+        sig = sig_mix(sig, k_sig_no_nee);
+    }
+    p.beta[pid] = make_float4(nb.x, nb.y, nb.z, 0.f);
+    if (p.sig) p.sig[pid] = sig;
+    o.next = cont;
+    if (cont) {
+        ff_ray_store(&p.ray_ff[3ull * pid], v.org, v.dir);
+        o.norg = ff3_f(v.org);
+        o.nd = ff3_f(v.dir);
+    }
+}
+
+// Enqueues the rays one shading step produced (all lanes of the warp call it).
+__device__ __forceinline__ void enqueue_shaded(bool active, int pid, int prim, const HitShade& o,
+                                               float4* __restrict__ shadow_q, int* __restrict__ shadow_count,
+                                               float4* __restrict__ next_q, int* __restrict__ next_count) {
+    const bool want_shadow = active && o.shadow;
+    const bool want_next = active && o.next && next_count != nullptr;
+    const int ps = warp_append(0xffffffffu, want_shadow, shadow_count);
+    if (want_shadow) {
+        shadow_q[3 * ps] = make_float4(o.so.x, o.so.y, o.so.z, __int_as_float(pid));
+        shadow_q[3 * ps + 1] = make_float4(o.sd.x, o.sd.y, o.sd.z, o.stmax);
+        shadow_q[3 * ps + 2] = make_float4(o.contrib.x, o.contrib.y, o.contrib.z, 0.f);
+    }
+    const int pn = warp_append(0xffffffffu, want_next, next_count);
+    if (want_next) {
+        next_q[2 * pn] = make_float4(o.norg.x, o.norg.y, o.norg.z, __int_as_float(pid));
+        next_q[2 * pn + 1] = make_float4(o.nd.x, o.nd.y, o.nd.z, __int_as_float(prim));
+    }
+}
+
+// Kahan-adds samples pid0, pid0 + stride, ... (n of them, in sample order) of one pixel to
+// its accumulators; records per-sample radiance and signatures when rec_rad is set.
+__device__ __forceinline__ void accumulate_pixel(const PathDev& p, uint32_t pid0, uint32_t stride, uint32_t n,
+                                                 float4* accum, float4* comp, float4* aov_a, float4* aov_n,
+                                                 float* rec_rad, uint32_t* rec_sig, size_t rec_idx) {
+    float4 sum = *accum, c = *comp, A = *aov_a, N = *aov_n;
+    for (uint32_t j = 0; j < n; ++j) {
+        const uint32_t pid = pid0 + j * stride;
+        const float4 L = p.lpath[pid];
+        kahan_add(sum.x, c.x, L.x);
+        kahan_add(sum.y, c.y, L.y);
+        kahan_add(sum.z, c.z, L.z);
+        const float4 a = p.aov_a[pid], nn = p.aov_n[pid];
+        A.x += a.x; A.y += a.y; A.z += a.z; A.w += a.w;
+        N.x += nn.x; N.y += nn.y; N.z += nn.z;
+        if (rec_rad) {
+            const size_t idx = rec_idx + j;
+            rec_rad[3 * idx] = L.x;
+            rec_rad[3 * idx + 1] = L.y;
+            rec_rad[3 * idx + 2] = L.z;
+            rec_sig[idx] = p.sig ? p.sig[pid] : 0u;
+        }
+    }
+    *accum = sum;
+    *comp = c;
+    *aov_a = A;
+    *aov_n = N;
+}
+
+// ------------------------------------------------------------------ one thread per path
+
+constexpr int k_adjoint_max_depth = 16;
+
+struct PathVertex {
+    int prim;
+    int light;
+    float gv;
+};
+
+// Traces one path sample; fills up to k_adjoint_max_depth vertices when `verts` is given.
+// Returns the radiance; writes first-hit AOVs and the signature when the pointers are set.
+// rays / shadow_rays are incremented per closest-hit / shadow ray traced.
+template <bool STATS>
+__device__ __forceinline__ float3 trace_path(const FrameParams& f, const SceneDev& s, uint32_t x, uint32_t y,
+                                             uint32_t sample, PathVertex* verts, int& n_verts, float4* aov_a,
+                                             float4* aov_n, uint32_t* sig_out, uint32_t& err, TraceCounters& cnt,
+                                             int& rays, int& shadow_rays) {
+    const VertexScene vs{s.tri_in, s.albedo, s.emission, s.emitters, s.n_emit, f.eps};
+    ff3 ro, rd;
+    camera_ray_ff(f, x, y, sample, ro, rd);
+    float3 beta = mk3(1.f, 1.f, 1.f), L = mk3(0.f, 0.f, 0.f);
+    uint32_t sig = 0;
+    int exclude = -1;
+    n_verts = 0;
+    for (uint32_t k = 1; k <= f.max_depth; ++k) {
+        const RayInv r = make_ray(ff3_f(ro), ff3_f(rd));
+        float t, bu, bv;
+        ++rays;
+        const int prim = trace_bvh<false, STATS>(s.nodes, s.tris, s.n_tris, r, __int_as_float(0x7f800000), exclude, t,
+                                                 bu, bv, err, cnt);
+        if (prim < 0) {
+            sig = sig_mix(sig, k_sig_miss);
+            break;
+        }
+        const float3 alb = xyz(__ldg(&s.albedo[prim]));
+        const float3 nb = beta * alb;
+        const bool cont = k < f.max_depth && max3(nb) > 0.0f;
+        VertexResult v;
+        shade_vertex(vs, path_key(f.seed, y * f.width + x, sample, k), prim, make_float4(t, 0.f, bu, bv), ro, rd, cont,
+                     v);
+        sig = sig_mix(sig, static_cast<uint32_t>(prim));
+        if (k == 1) {
+            const float3 em = xyz(__ldg(&s.emission[prim]));
+            L = em;
+            if (aov_a) first_hit_aovs(alb, em, t, v.nrm, *aov_a, *aov_n);
+        }
+        float gv = 0.0f;
+        if (v.nee) {
+            const RayInv sr = make_ray(v.so, v.sd);
+            float st2, su, sv;
+            ++shadow_rays;
+            const int occ = trace_bvh<true, STATS>(s.nodes, s.tris, s.n_tris, sr, v.stmax, -1, st2, su, sv, err, cnt);
+            if (occ < 0) {
+                // The same product and the same unfused add as the wavefront's shadow kernel.
+                const float3 cb = beta * alb * xyz(__ldg(&s.emission[v.light])) * v.g;
+                L = mk3(__fadd_rn(L.x, cb.x), __fadd_rn(L.y, cb.y), __fadd_rn(L.z, cb.z));
+                gv = v.g;
+                sig = sig_mix(sig, k_sig_lit);
+            } else {
+                sig = sig_mix(sig, k_sig_shadowed);
+            }
+        } else {
+            sig = sig_mix(sig, k_sig_no_nee);
+        }
+        if (verts && n_verts < k_adjoint_max_depth) verts[n_verts] = PathVertex{prim, v.nee ? v.light : -1, gv};
+        ++n_verts;
+        beta = nb;
+        if (!cont) break;
+        ro = v.org;
+        rd = v.dir;
+        exclude = prim;
+    }
+    if (sig_out) *sig_out = sig;
+    return L;
+}
+
+// Path-replay adjoint of one path sample with pixel adjoint d (= dLoss/dI_pixel / spp).
+// With vertices k = 1..K on triangles h_k (albedo rho_k), NEE lights l_k with factors gv_k
+// (g times visibility, 0 without an unoccluded light sample) and throughput
+// beta_k = prod_{j<k} rho_j:
+//   radiance = Le(h_1) + sum_k beta_k rho_k Le(l_k) gv_k
+//   dL/dLe(h_1)  += d
+//   dL/dLe(l_k)  += d beta_k rho_k gv_k
+//   dL/drho(h_k) += d beta_k H_k,  H_k = Le(l_k) gv_k + rho_{k+1} H_{k+1},  H_{K+1} = 0
+// (all products per colour channel). H_k needs no division by albedo, so zero albedos are
+// exact. The vertex records of the path (at most k_adjoint_max_depth) live in local memory.
+// `rays` is incremented by the rays the replay traces.
+__device__ __forceinline__ void adjoint_path(const FrameParams& f, const SceneDev& s, uint32_t x, uint32_t y,
+                                             uint32_t sample, float3 d, float* __restrict__ grad_albedo,
+                                             float* __restrict__ grad_emission, uint32_t& err, TraceCounters& cnt,
+                                             int& rays) {
+    PathVertex verts[k_adjoint_max_depth];
+    float3 H[k_adjoint_max_depth];
+    int nv = 0, shadow_rays = 0;
+    trace_path<false>(f, s, x, y, sample, verts, nv, nullptr, nullptr, nullptr, err, cnt, rays, shadow_rays);
+    rays += shadow_rays;
+    nv = min(nv, k_adjoint_max_depth);
+    if (nv == 0) return;
+    atomicAdd(&grad_emission[3 * verts[0].prim + 0], d.x);
+    atomicAdd(&grad_emission[3 * verts[0].prim + 1], d.y);
+    atomicAdd(&grad_emission[3 * verts[0].prim + 2], d.z);
+    float3 next = mk3(0.f, 0.f, 0.f);
+    for (int k = nv - 1; k >= 0; --k) {
+        float3 h = mk3(0.f, 0.f, 0.f);
+        if (verts[k].light >= 0 && verts[k].gv != 0.0f) h = xyz(__ldg(&s.emission[verts[k].light])) * verts[k].gv;
+        if (k + 1 < nv) h += xyz(__ldg(&s.albedo[verts[k + 1].prim])) * next;
+        H[k] = h;
+        next = h;
+    }
+    float3 beta = mk3(1.f, 1.f, 1.f);
+    for (int k = 0; k < nv; ++k) {
+        const int h = verts[k].prim;
+        const float3 rho = xyz(__ldg(&s.albedo[h]));
+        const float3 ga = d * beta * H[k];
+        atomicAdd(&grad_albedo[3 * h + 0], ga.x);
+        atomicAdd(&grad_albedo[3 * h + 1], ga.y);
+        atomicAdd(&grad_albedo[3 * h + 2], ga.z);
+        if (verts[k].light >= 0 && verts[k].gv != 0.0f) {
+            const float3 ge = d * beta * rho * verts[k].gv;
+            atomicAdd(&grad_emission[3 * verts[k].light + 0], ge.x);
+            atomicAdd(&grad_emission[3 * verts[k].light + 1], ge.y);
+            atomicAdd(&grad_emission[3 * verts[k].light + 2], ge.z);
+        }
+        beta = beta * rho;
+    }
+}
+
+}  // namespace quasi

@@ -10,6 +10,7 @@
 // The scene and options come from the environment at create time (QUASI_SCENE,
 // QUASI_INTEGRATOR, QUASI_SPP, QUASI_DEPTH, QUASI_SEED) or later from Q_cuda_set_*.
 #include "../../include/quasi_cuda.h"
+#include "batch.hpp"
 #include "renderer.hpp"
 
 #include <cuda_runtime.h>
@@ -304,6 +305,103 @@ Q_CUDA_EXPORT int Q_cuda_backward(Q_plugin_handle* handle, const float* device_g
 Q_CUDA_EXPORT int Q_cuda_autotune(Q_plugin_handle* handle, double budget_ms) {
     Q_STATE_OR_FAIL(handle);
     return r->autotune(budget_ms);
+}
+
+// ------------------------------------------------------------------ scene batches
+
+Q_CUDA_EXPORT int Q_cuda_batch_create(Q_plugin_handle* handle, const Q_cuda_batch_scene* scenes, uint32_t count,
+                                      const Q_cuda_batch_options* options, Q_cuda_batch** out) {
+    Q_STATE_OR_FAIL(handle);
+    if (!out) return QUASI_ERR_INVALID;
+    *out = nullptr;
+    quasi::BatchRenderer* b = new (std::nothrow) quasi::BatchRenderer(*r);
+    if (!b) return QUASI_ERR_OOM;
+    const int rc = b->create(scenes, count, options);
+    if (rc) {
+        r->fail(rc, "batch: " + b->last_error());
+        delete b;
+        return rc;
+    }
+    *out = reinterpret_cast<Q_cuda_batch*>(b);
+    return QUASI_OK;
+}
+
+#define Q_BATCH_OR_FAIL(batch)              \
+    if (!(batch)) return QUASI_ERR_INVALID; \
+    quasi::BatchRenderer* b = reinterpret_cast<quasi::BatchRenderer*>(batch)
+
+Q_CUDA_EXPORT void Q_cuda_batch_destroy(Q_cuda_batch* batch) { delete reinterpret_cast<quasi::BatchRenderer*>(batch); }
+
+Q_CUDA_EXPORT int Q_cuda_batch_set_options(Q_cuda_batch* batch, const Q_cuda_batch_options* options) {
+    Q_BATCH_OR_FAIL(batch);
+    if (!options) return QUASI_ERR_INVALID;
+    return b->set_options(*options);
+}
+
+Q_CUDA_EXPORT int Q_cuda_batch_get_options(Q_cuda_batch* batch, Q_cuda_batch_options* options) {
+    Q_BATCH_OR_FAIL(batch);
+    if (!options) return QUASI_ERR_INVALID;
+    *options = b->options();
+    return QUASI_OK;
+}
+
+Q_CUDA_EXPORT int Q_cuda_batch_render(Q_cuda_batch* batch, void* stream) {
+    Q_BATCH_OR_FAIL(batch);
+    return b->render(static_cast<cudaStream_t>(stream));
+}
+
+Q_CUDA_EXPORT int Q_cuda_batch_reset(Q_cuda_batch* batch) {
+    Q_BATCH_OR_FAIL(batch);
+    return b->reset();
+}
+
+Q_CUDA_EXPORT int Q_cuda_batch_synchronize(Q_cuda_batch* batch) {
+    Q_BATCH_OR_FAIL(batch);
+    return b->synchronize();
+}
+
+Q_CUDA_EXPORT int Q_cuda_batch_get_stats(Q_cuda_batch* batch, Q_cuda_batch_stats* stats) {
+    Q_BATCH_OR_FAIL(batch);
+    return b->stats(stats);
+}
+
+Q_CUDA_EXPORT int Q_cuda_batch_readback(Q_cuda_batch* batch, uint32_t index, float* host_rgba) {
+    Q_BATCH_OR_FAIL(batch);
+    return b->readback(index, host_rgba);
+}
+
+Q_CUDA_EXPORT int Q_cuda_batch_resolve_device(Q_cuda_batch* batch, float* device_rgb, void* stream) {
+    Q_BATCH_OR_FAIL(batch);
+    return b->resolve_device(device_rgb, static_cast<cudaStream_t>(stream));
+}
+
+Q_CUDA_EXPORT int Q_cuda_batch_offsets(Q_cuda_batch* batch, uint32_t index, uint64_t* tri_offset,
+                                       uint64_t* px_offset) {
+    Q_BATCH_OR_FAIL(batch);
+    return b->offsets(index, tri_offset, px_offset);
+}
+
+Q_CUDA_EXPORT int Q_cuda_batch_set_materials_device(Q_cuda_batch* batch, const float* device_albedo,
+                                                    const float* device_emission, void* stream) {
+    Q_BATCH_OR_FAIL(batch);
+    return b->set_materials_device(device_albedo, device_emission, static_cast<cudaStream_t>(stream));
+}
+
+Q_CUDA_EXPORT int Q_cuda_batch_backward(Q_cuda_batch* batch, const float* device_grad_image,
+                                        float* device_grad_albedo, float* device_grad_emission, void* stream) {
+    Q_BATCH_OR_FAIL(batch);
+    return b->backward(device_grad_image, device_grad_albedo, device_grad_emission,
+                       static_cast<cudaStream_t>(stream));
+}
+
+Q_CUDA_EXPORT int Q_cuda_batch_autotune(Q_cuda_batch* batch, double budget_ms, Q_cuda_batch_options* chosen) {
+    Q_BATCH_OR_FAIL(batch);
+    return b->autotune(budget_ms, chosen);
+}
+
+Q_CUDA_EXPORT const char* Q_cuda_batch_last_error(Q_cuda_batch* batch) {
+    if (!batch) return "null batch";
+    return reinterpret_cast<quasi::BatchRenderer*>(batch)->last_error().c_str();
 }
 
 }  // extern "C"

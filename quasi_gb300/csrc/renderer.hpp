@@ -73,6 +73,8 @@ public:
     uint32_t height() const { return height_; }
     bool has_scene() const { return has_scene_; }
     cudaStream_t stream() const { return stream_; }
+    int device() const { return device_; }
+    int sm_count() const { return sm_count_; }
     const std::string& last_error() const { return error_; }
     int fail(int code, const std::string& msg) {
         error_ = msg;

@@ -17,6 +17,8 @@ namespace {
 
 inline uint32_t ceil_div(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
 
+}  // namespace
+
 CameraFF make_camera_basis(const Q_camera& c, uint32_t w, uint32_t h) {
     // plugin.mm:649-674 (host direction) and plugin.mm:134-147 (shader basis), in double.
     double dir[3] = {double(c.target[0]) - c.position[0], double(c.target[1]) - c.position[1],
@@ -52,8 +54,6 @@ CameraFF make_camera_basis(const Q_camera& c, uint32_t w, uint32_t h) {
     split(LL, b.ll_hi, b.ll_lo);
     return b;
 }
-
-}  // namespace
 
 // Reference-integrator entry point (refmode.cu).
 cudaError_t launch_reference_frame(const float4* quads, uint32_t n_quads, const Q_camera& cam, uint32_t width,
@@ -553,7 +553,8 @@ int Renderer::backward(const float* grad_image, uint32_t spp, uint32_t sample_ba
     const int grid = sm_count_ * std::max(occ, 1);
     R_TRY(QUASI_LAUNCH(prof_, "adjoint", s,
                        (k_adjoint<<<grid, 128, 0, s>>>(f, sd, grad_image, 1.0f / static_cast<float>(spp), grad_albedo,
-                                                      grad_emission, counters_.as<int>(), err_dev_.as<uint32_t>()))),
+                                                      grad_emission, counters_.as<int>(), err_dev_.as<uint32_t>(),
+                                                      stats_dev_.as<unsigned long long>()))),
           "adjoint");
     return QUASI_OK;
 }
@@ -661,6 +662,9 @@ int Renderer::stats(Q_cuda_stats* out) {
         st = last_stats_;
     }
     st.total_rays = stats_host_[4];
+    unsigned long long adj = 0;
+    R_TRY(cudaMemcpy(&adj, stats_dev_.as<unsigned long long>() + 7, sizeof(adj), cudaMemcpyDeviceToHost), "d2h");
+    st.adjoint_rays = adj;
     st.samples_accumulated = samples_;
     st.kernel_launches = prof_.launches();
     st.error_flags = err_host_ ? *err_host_ : 0u;

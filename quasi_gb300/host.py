@@ -315,3 +315,110 @@ class PluginHost:
 
     def autotune(self, budget_ms: float = 2000.0) -> None:
         self._check("Q_cuda_autotune", self.lib.Q_cuda_autotune(self.handle, budget_ms))
+
+
+class Batch:
+    """A set of scenes rendered together (Q_cuda_batch_*), owned by a PluginHost.
+
+    scenes: list of (Scene, width, height, spp). Each frame renders spp samples of every
+    pixel of every scene; images are bit-identical to rendering each scene alone with the
+    same seed, depth and ray_eps.
+    """
+
+    def __init__(self, host: PluginHost, scenes, **options):
+        self.host = host
+        self.lib = host.lib
+        self.sizes = [(int(w), int(h), int(spp)) for _, w, h, spp in scenes]
+        self._keep = []
+        cs = []
+        for sc, w, h, spp in scenes:
+            c, keep = sc.to_c()
+            self._keep.append((c, keep))
+            cs.append(c)
+        arr = (A.Q_cuda_batch_scene * len(cs))()
+        for i, (c, (w, h, spp)) in enumerate(zip(cs, self.sizes)):
+            arr[i].scene = C.pointer(c)
+            arr[i].width, arr[i].height, arr[i].spp = w, h, spp
+        o = A.Q_cuda_batch_options()
+        for k, v in options.items():
+            if not hasattr(o, k):
+                raise AttributeError(k)
+            setattr(o, k, v)
+        out = C.c_void_p()
+        rc = self.lib.Q_cuda_batch_create(host.handle, arr, len(cs), C.byref(o), C.byref(out))
+        host._check("Q_cuda_batch_create", rc)
+        self._keep = None  # the batch copied the scenes
+        self.handle = out
+        self.tri_counts = [sc.tri_count for sc, *_ in scenes]
+
+    def destroy(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.Q_cuda_batch_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.destroy()
+
+    def _check(self, call: str, rc: int) -> None:
+        if rc != A.QUASI_OK:
+            detail = self.lib.Q_cuda_batch_last_error(self.handle)
+            raise QuasiError(call, rc, detail.decode(errors="replace") if detail else "")
+
+    def options(self) -> A.Q_cuda_batch_options:
+        o = A.Q_cuda_batch_options()
+        self._check("Q_cuda_batch_get_options", self.lib.Q_cuda_batch_get_options(self.handle, C.byref(o)))
+        return o
+
+    def set_options(self, **kw) -> None:
+        o = self.options()
+        for k, v in kw.items():
+            if not hasattr(o, k):
+                raise AttributeError(k)
+            setattr(o, k, v)
+        self._check("Q_cuda_batch_set_options", self.lib.Q_cuda_batch_set_options(self.handle, C.byref(o)))
+
+    def render(self, stream: int | None = None) -> None:
+        self._check("Q_cuda_batch_render", self.lib.Q_cuda_batch_render(self.handle, stream))
+
+    def reset(self) -> None:
+        self._check("Q_cuda_batch_reset", self.lib.Q_cuda_batch_reset(self.handle))
+
+    def synchronize(self) -> None:
+        self._check("Q_cuda_batch_synchronize", self.lib.Q_cuda_batch_synchronize(self.handle))
+
+    def stats(self) -> A.Q_cuda_batch_stats:
+        s = A.Q_cuda_batch_stats()
+        self._check("Q_cuda_batch_get_stats", self.lib.Q_cuda_batch_get_stats(self.handle, C.byref(s)))
+        return s
+
+    def readback(self, index: int) -> np.ndarray:
+        w, h, _ = self.sizes[index]
+        out = np.zeros((h, w, 4), np.float32)
+        self._check("Q_cuda_batch_readback", self.lib.Q_cuda_batch_readback(self.handle, index, out.ctypes.data))
+        return out
+
+    def offsets(self, index: int) -> tuple[int, int]:
+        t, p = C.c_uint64(), C.c_uint64()
+        self._check("Q_cuda_batch_offsets", self.lib.Q_cuda_batch_offsets(self.handle, index, C.byref(t), C.byref(p)))
+        return int(t.value), int(p.value)
+
+    def resolve_device(self, device_rgb: int, stream: int | None = None) -> None:
+        self._check("Q_cuda_batch_resolve_device", self.lib.Q_cuda_batch_resolve_device(self.handle, device_rgb, stream))
+
+    def set_materials_device(self, albedo_ptr: int | None, emission_ptr: int | None, stream: int | None = None) -> None:
+        self._check("Q_cuda_batch_set_materials_device",
+                    self.lib.Q_cuda_batch_set_materials_device(self.handle, albedo_ptr, emission_ptr, stream))
+
+    def backward(self, grad_image_ptr: int, grad_albedo_ptr: int | None, grad_emission_ptr: int | None,
+                 stream: int | None = None) -> None:
+        self._check("Q_cuda_batch_backward", self.lib.Q_cuda_batch_backward(self.handle, grad_image_ptr,
+                                                                            grad_albedo_ptr, grad_emission_ptr,
+                                                                            stream))
+
+    def autotune(self, budget_ms: float = 5000.0) -> A.Q_cuda_batch_options:
+        o = A.Q_cuda_batch_options()
+        self._check("Q_cuda_batch_autotune", self.lib.Q_cuda_batch_autotune(self.handle, budget_ms, C.byref(o)))
+        return o

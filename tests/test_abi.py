@@ -48,7 +48,8 @@ def test_struct_layouts_match_c_compiler(tmp_path):
                "Q_readback_result": A.Q_readback_result, "Q_aov_buffer": A.Q_aov_buffer,
                "Q_readback_aov_result": A.Q_readback_aov_result, "Q_cuda_scene": A.Q_cuda_scene,
                "Q_cuda_options": A.Q_cuda_options, "Q_cuda_stats": A.Q_cuda_stats,
-               "Q_cuda_kernel_time": A.Q_cuda_kernel_time}
+               "Q_cuda_kernel_time": A.Q_cuda_kernel_time, "Q_cuda_batch_scene": A.Q_cuda_batch_scene,
+               "Q_cuda_batch_options": A.Q_cuda_batch_options, "Q_cuda_batch_stats": A.Q_cuda_batch_stats}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void) {"]
     for name, cls in structs.items():
         lines.append(f'printf("{name} %zu\\n", sizeof({name}));')

@@ -84,8 +84,9 @@ def test_adjoint_matches_central_finite_differences(torch_mod):
 
     rng = np.random.default_rng(3)
     # Central differences of an FP32 image resolve a gradient only above the image's rounding
-    # noise, so the 64 entries are drawn from those above 1e-3 of the largest.
-    cand = np.argwhere(np.abs(ga) > 1e-3 * np.abs(ga).max())
+    # noise (an entry at 1e-3 of the largest gradient already shows 2e-3 relative noise), so
+    # the 64 entries are drawn from those above 1e-2 of the largest.
+    cand = np.argwhere(np.abs(ga) > 1e-2 * np.abs(ga).max())
     picks = cand[rng.choice(len(cand), size=min(64, len(cand)), replace=False)]
     assert len(picks) == 64
     errs = []
