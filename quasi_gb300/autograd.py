@@ -125,9 +125,11 @@ def fit_albedo(batch: Batch, target: torch.Tensor, albedo0: torch.Tensor, emissi
                lr: float = 0.01) -> tuple[torch.Tensor, list[float]]:
     """Adam on the per-triangle albedo of every scene of the batch against target images
     (L2 loss, mean over pixels and channels); albedo is kept in [0, 1] after each step.
+    Adam's eps is 1e-15: the gradients of these mostly dark images are ~1e-10, far below the
+    usual 1e-8, which would otherwise shrink every step by that ratio.
     Returns the fitted albedo and the loss of every step."""
     albedo = albedo0.detach().clone().requires_grad_(True)
-    opt = torch.optim.Adam([albedo], lr=lr)
+    opt = torch.optim.Adam([albedo], lr=lr, eps=1e-15)
     px = int(batch.stats().px_total)
     losses = []
     for _ in range(steps):

@@ -96,8 +96,8 @@ def build_headless() -> Path | None:
         return HEADLESS
     libdir = _cuda_lib_dir()
     srcs = [str(p) for p in sorted(HOST.glob("*.cpp"))]
-    _run(["g++", "-std=c++20", "-O2", "-Wall", "-Wextra", "-I", str(ROOT / "include"), "-I", str(CUDA_HOME / "include"),
-          *srcs, "-o", str(HEADLESS), "-ldl", "-L", str(libdir), "-lcudart", "-Xlinker", f"-rpath,{libdir}"])
+    _run(["g++", "-std=c++23", "-O2", "-Wall", "-Wextra", "-I", str(ROOT / "include"), "-I", str(CUDA_HOME / "include"),
+          *srcs, "-o", str(HEADLESS), "-ldl", "-L", str(libdir), "-lcudart", f"-Wl,-rpath,{libdir}"])
     return HEADLESS
 
 

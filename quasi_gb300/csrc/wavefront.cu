@@ -6,6 +6,7 @@
 #include "megakernel.cuh"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 
@@ -695,6 +696,84 @@ int Renderer::kernel_times(Q_cuda_kernel_time* out, uint32_t capacity, uint32_t*
     return QUASI_OK;
 }
 
-int Renderer::autotune(double) { return fail(QUASI_ERR_INVALID, "autotuner not built"); }
+// Coordinate search over the renderer form, wave size, trace block size and treelet depth,
+// timing short progressive frames (at most 8 spp, LBVH kept) with the frame events.
+int Renderer::autotune(double budget_ms) {
+    if (!has_scene_ || width_ == 0 || height_ == 0) return fail(QUASI_ERR_STATE, "render a frame before autotune");
+    if (opt_.integrator != QUASI_INTEGRATOR_NEE) return fail(QUASI_ERR_STATE, "autotune needs the NEE integrator");
+    if (budget_ms <= 0.0) budget_ms = 2000.0;
+    const auto t0 = std::chrono::steady_clock::now();
+    auto elapsed = [&]() {
+        return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    };
+    const Q_cuda_options saved = opt_;
+    Q_cuda_options base = opt_;
+    base.spp_per_frame = std::min<uint32_t>(saved.spp_per_frame, 8);
+    base.rebuild_each_frame = 0;
+    base.record_samples = 0;
+    base.collect_stats = 0;
+    base.profile = 0;
+    const uint32_t slots = ceil_div(width_, 8) * ceil_div(height_, 4) * 32;
+    if (base.wave_spp == 0) base.wave_spp = effective_wave_spp(base.spp_per_frame);
+    Q_render_frame fr{};
+    fr.width = width_;
+    fr.height = height_;
+    fr.camera = camera_;
+    auto measure = [&](const Q_cuda_options& o, float& ms) -> int {
+        if (o.smem_levels != opt_.smem_levels) bvh_dirty_ = true;  // rebuild the treelet (untimed frame)
+        opt_ = o;
+        prof_.set_enabled(false);
+        for (int rep = 0; rep < 2; ++rep) {
+            const int rc = render(fr);
+            if (rc) return rc;
+        }
+        R_TRY(cudaEventSynchronize(ev_frame1_), "sync");
+        R_TRY(cudaEventElapsedTime(&ms, ev_frame0_, ev_frame1_), "event time");
+        return QUASI_OK;
+    };
+    Q_cuda_options best = base;
+    float best_ms = 0.f;
+    int rc = measure(best, best_ms);
+    if (rc) {
+        opt_ = saved;
+        return rc;
+    }
+    for (int dim = 0; dim < 4 && elapsed() < budget_ms; ++dim) {
+        std::vector<uint32_t> vals;
+        if (dim == 0) vals = {0u, 1u};
+        if (dim == 1)
+            for (uint32_t target : {2u << 20, 4u << 20, 8u << 20, 16u << 20})
+                vals.push_back(std::max<uint32_t>(1, std::min<uint32_t>(base.spp_per_frame, target / slots)));
+        if (dim == 2) vals = {64u, 128u, 256u};
+        if (dim == 3) vals = {0u, 7u, 32u};
+        for (uint32_t v : vals) {
+            if (elapsed() >= budget_ms) break;
+            Q_cuda_options o = best;
+            uint32_t& field = dim == 0 ? o.megakernel : dim == 1 ? o.wave_spp : dim == 2 ? o.trace_block : o.smem_levels;
+            if (field == v || (dim == 2 && field == 0 && v == 128)) continue;
+            if (dim == 2 && o.megakernel) continue;  // the megakernel runs 128-thread blocks
+            if (dim == 3 && o.megakernel) continue;
+            field = v;
+            float ms = 0.f;
+            rc = measure(o, ms);
+            if (rc) {
+                opt_ = saved;
+                return rc;
+            }
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = o;
+            }
+        }
+    }
+    opt_ = saved;
+    opt_.megakernel = best.megakernel;
+    opt_.wave_spp = best.wave_spp;
+    opt_.trace_block = best.trace_block;
+    opt_.smem_levels = best.smem_levels;
+    prof_.set_enabled(opt_.profile != 0);
+    bvh_dirty_ = true;  // the treelet depth may have changed
+    return reset();
+}
 
 }  // namespace quasi

@@ -229,3 +229,22 @@ def test_tonemap_into_device_buffer(host):
     expect = np.clip(np.power(hdr / (hdr + 1.0), 1.0 / 2.2) * 255.0 + 0.5, 0, 255).astype(np.uint8)
     assert np.abs(ldr[..., :3].astype(int) - expect.astype(int)).max() <= 1
     assert np.all(ldr[..., 3] == 255)
+
+
+def test_autotune_keeps_images(cuda_ok):
+    """Q_cuda_autotune picks among bit-identical forms and launch shapes: the first frame after
+    it (accumulation reset) equals the first frame before it."""
+    sc = q.make_scene("soup:n=50000,seed=3")
+    h = q.PluginHost(width=160, height=96)
+    h.set_scene(sc)
+    h.set_options(spp_per_frame=16, max_depth=6, seed=0)
+    h.render(160, 96, dirty=True)
+    ref = h.readback()
+    h.autotune(1500)
+    o = h.options()
+    assert o.megakernel in (0, 1) and o.trace_block in (0, 64, 128, 256) and o.smem_levels in (0, 7, 32)
+    assert o.spp_per_frame == 16 and o.max_depth == 6 and o.wave_spp in (1, 2, 4, 8, 16)
+    h.render(160, 96)
+    assert np.array_equal(h.readback(), ref)
+    assert h.stats().error_flags == 0
+    h.destroy()
