@@ -30,7 +30,8 @@ METRIC = "Mrays/s at 1080p 64spp 1M tris; batched & backward Mrays/s at rel errâ
 SCENE = "soup:n=1000000,seed=0"
 WIDTH, HEIGHT, SPP, DEPTH = 1920, 1080, 64, 8
 WORKLOAD = "soup-1M 1920x1080 64spp depth8 NEE, LBVH rebuilt every frame"
-NODE_BYTES, TRI_BYTES, RAY_BYTES, HIT_BYTES, SHADOW_BYTES = 64, 48, 32, 16, 48
+TRI_BYTES, RAY_BYTES, HIT_BYTES, SHADOW_BYTES = 48, 32, 16, 48
+NODE_BYTES = {2: 64, 8: 96}  # binary LBVH node / 8-wide record
 
 
 def _peaks() -> tuple[float, str]:
@@ -172,7 +173,8 @@ def bench_batch(host, stream, flush, steps: int, warmup: int, budget_ms: float) 
         chosen = b.autotune(budget_ms)
         res["autotune_s"] = time.perf_counter() - t0
         res["autotuned"] = {"form": ["wavefront", "megakernel"][chosen.form], "wave_paths": chosen.wave_paths,
-                            "trace_block": chosen.trace_block, "fetch_rays": chosen.fetch_rays}
+                            "trace_block": chosen.trace_block, "fetch_rays": chosen.fetch_rays,
+                            "refill_lanes": chosen.refill_lanes, "bvh_width": chosen.bvh_width}
         for _ in range(warmup):
             b.render(h)
         b.synchronize()
@@ -357,7 +359,8 @@ def run_ours(args) -> None:
     scene = q.make_scene(SCENE, host.lib)
     host.set_scene(scene)
     opts = dict(spp_per_frame=SPP, max_depth=DEPTH, rebuild_each_frame=1, record_samples=0, wave_spp=args.wave_spp,
-                trace_block=args.trace_block)
+                trace_block=args.trace_block, bvh_width=args.bvh_width, refill_lanes=args.refill_lanes)
+    node_bytes = NODE_BYTES[2 if args.bvh_width == 2 else 8]
     host.set_options(seed=0, **opts)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
@@ -373,8 +376,8 @@ def run_ours(args) -> None:
     cs = host.stats()
     host.set_options(seed=0, collect_stats=0, **opts)
     closest_rays = cs.camera_rays + cs.extension_rays
-    alg_closest = closest_rays * (RAY_BYTES + HIT_BYTES) + cs.node_visits * NODE_BYTES + cs.tri_tests * TRI_BYTES
-    alg_shadow = cs.shadow_rays * SHADOW_BYTES + cs.shadow_node_visits * NODE_BYTES + cs.shadow_tri_tests * TRI_BYTES
+    alg_closest = closest_rays * (RAY_BYTES + HIT_BYTES) + cs.node_visits * node_bytes + cs.tri_tests * TRI_BYTES
+    alg_shadow = cs.shadow_rays * SHADOW_BYTES + cs.shadow_node_visits * node_bytes + cs.shadow_tri_tests * TRI_BYTES
 
     for i in range(args.warmup):
         step(i)
@@ -438,20 +441,32 @@ def run_ours(args) -> None:
     frames = args.steps
     alg = {"trace_closest": alg_closest, "trace_shadow": alg_shadow}.get(name)
     achieved = (alg * frames / (kms / 1e3) / 1e9) if alg is not None and kms > 0 else None
-    traffic = None
+    # DRAM traffic per launch: bytes per ray from a committed ncu capture (a smaller image of
+    # the same scene) times the rays of an average launch here
+    traffic = traffic_note = None
     tf = ROOT / "profiles" / "trace_traffic.json"
-    if tf.exists():
+    rays_of = {"trace_closest": closest_rays, "trace_shadow": cs.shadow_rays}
+    if tf.exists() and name in rays_of:
         try:
-            traffic = json.loads(tf.read_text()).get(name)
+            entry = json.loads(tf.read_text()).get(name)
+            if entry:
+                traffic = entry["dram_bytes_per_ray"] * rays_of[name] * frames / n_launch
+                traffic_note = entry["source"] + "; " + entry["scaling"]
         except Exception:
             traffic = None
     frame_ms = total_ms / args.steps
     share = {k: round(v[1] / max(sum(x[1] for x in times.values()), 1e-9), 4) for k, v in times.items()}
     roofline = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": (achieved / peak) if achieved else None, "peak_source": f"{peak_kind} hbm_gbs",
-                "traffic": traffic, "alg_bytes_per_launch": (alg * frames / n_launch) if alg else None,
+                "traffic": traffic, "traffic_source": traffic_note,
+                "alg_bytes_per_launch": (alg * frames / n_launch) if alg else None,
                 "avg_launch_ms": kms / n_launch, "launches": n_launch, "kernel_share": share,
-                "bytes_model": "closest: rays*(32+16) + node_visits*64 + tri_tests*48; shadow: rays*48 + node_visits*64 + tri_tests*48 (counted in an untimed frame)"}
+                "bytes_model": f"closest: rays*(32+16) + node_visits*{node_bytes} + tri_tests*48; shadow: rays*48 + "
+                               f"node_visits*{node_bytes} + tri_tests*48 (counted in an untimed frame)",
+                "per_ray": {"closest_node_visits": cs.node_visits / max(closest_rays, 1),
+                            "closest_tri_tests": cs.tri_tests / max(closest_rays, 1),
+                            "shadow_node_visits": cs.shadow_node_visits / max(cs.shadow_rays, 1),
+                            "shadow_tri_tests": cs.shadow_tri_tests / max(cs.shadow_rays, 1)}}
 
     batch = diff = None
     if rank == 0 and not args.no_batch:
@@ -472,7 +487,8 @@ def run_ours(args) -> None:
                            "spp": SPP, "max_depth": DEPTH, "rays_per_step": rays / args.steps / world,
                            "bvh_ms": st.bvh_ms, "l2": "flushed before every step (256 MiB write, inside the "
                            "timed region)", "parallelism": f"replicas x{world}", "wave_spp": args.wave_spp,
-                           "trace_block": args.trace_block},
+                           "trace_block": args.trace_block, "refill_lanes": args.refill_lanes,
+                           "bvh": "binary LBVH" if args.bvh_width == 2 else "8-wide records collapsed from the LBVH"},
                 "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
                 "clocks": clocks.summary(), "batch": batch, "diff": diff}
         print(json.dumps(line), flush=True)
@@ -489,6 +505,10 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--wave-spp", type=int, default=0)
     ap.add_argument("--trace-block", type=int, default=0)
+    ap.add_argument("--refill-lanes", type=int, default=0,
+                    help="trace kernels refill a warp once this many lanes are idle (0 = library default)")
+    ap.add_argument("--bvh-width", type=int, default=0, choices=[0, 2, 8],
+                    help="traversal structure: 8-wide records (0, 8) or the binary LBVH (2)")
     ap.add_argument("--ref-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

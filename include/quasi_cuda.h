@@ -196,8 +196,11 @@ typedef struct Q_cuda_options {
                                     (0 = default 5, 1..9, 32 = none) */
     float ray_eps;               /* ray origin offset along the normal (1e-4) */
     uint32_t refill_lanes;       /* trace kernels refill a warp once this many lanes idle
-                                    (1..32; 32 = refill only whole warps; 0 = default) */
+                                    (1..32; 32 = refill only whole warps; 0 = default:
+                                    4 for the 8-wide records, 32 for the binary LBVH) */
     uint32_t trace_steps;        /* node visits per lane between refill checks (0 = default) */
+    uint32_t bvh_width;          /* traversal structure: 8 = 8-wide records collapsed from the
+                                    LBVH (default, 0), 2 = the binary LBVH nodes */
 } Q_cuda_options;
 
 /* Counters of the last frame (rays actually traced) and of the whole accumulation. */
@@ -265,6 +268,11 @@ Q_CUDA_EXPORT const char* Q_cuda_last_error(Q_plugin_handle* handle);
  *   bounds    [6]        centroid bounds lo.xyz hi.xyz used for quantisation */
 Q_CUDA_EXPORT int Q_cuda_read_bvh(Q_plugin_handle* handle, uint32_t* morton, uint32_t* order,
                                   int32_t* children, float* boxes, float* bounds);
+/* Copies the 8-wide traversal records collapsed from the LBVH: 24 words (96 bytes) per
+ * internal node (max(n - 1, 1) records; layout in csrc/wide.cuh). Record 0 is the root; only
+ * records reachable from it through internal child references are used. No reference
+ * counterpart: the reference traces by brute force (plugin.mm:199-212). */
+Q_CUDA_EXPORT int Q_cuda_read_wide_bvh(Q_plugin_handle* handle, uint32_t* words);
 
 /* With record_samples: copies the last frame's per-sample radiance (width*height*spp*3,
  * ordered pixel-major then sample) and path signatures (width*height*spp). */
@@ -356,6 +364,9 @@ typedef struct Q_cuda_batch_options {
     uint32_t use_graph;     /* 0 = default (graph), 1 = graph, 2 = plain launches */
     uint32_t collect_stats; /* count BVH node visits and triangle tests */
     float ray_eps;          /* ray origin offset along the normal (1e-4) */
+    uint32_t bvh_width;     /* 8 = 8-wide traversal records (default, 0), 2 = binary LBVH */
+    uint32_t refill_lanes;  /* 8-wide trace kernels refill a warp once this many lanes are
+                               idle (1..32; 0 = default) */
 } Q_cuda_batch_options;
 
 typedef struct Q_cuda_batch_stats {

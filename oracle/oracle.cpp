@@ -120,6 +120,7 @@ struct Lbvh {
     std::vector<uint32_t> order;    // sorted position -> original index
     std::vector<int32_t> child;     // 2 per internal node
     std::vector<float> box;         // 12 per internal node: c0 lo hi, c1 lo hi
+    std::vector<int32_t> range;     // 2 per internal node: first and last leaf covered
 };
 
 inline uint32_t spread_bits(uint32_t q) {
@@ -178,6 +179,7 @@ void build_lbvh(uint32_t n, const float* v, Lbvh& b) {
     const uint32_t nodes = n > 1 ? n - 1 : 1;
     b.child.assign(2ull * nodes, 0);
     b.box.assign(12ull * nodes, 0.f);
+    b.range.assign(2ull * nodes, 0);
     auto leaf_box = [&](int pos, float* out) {
         const float* t = v + 9ull * b.order[pos];
         for (int a = 0; a < 3; ++a) {
@@ -215,6 +217,8 @@ void build_lbvh(uint32_t n, const float* v, Lbvh& b) {
         const int right = (it.hi == gamma + 1) ? ~(gamma + 1) : gamma + 1;
         b.child[2ull * it.idx] = left;
         b.child[2ull * it.idx + 1] = right;
+        b.range[2ull * it.idx] = it.lo;
+        b.range[2ull * it.idx + 1] = it.hi;
         post.push_back(it.idx);
         if (left >= 0) stack.push_back({left, it.lo, gamma});
         if (right >= 0) stack.push_back({right, gamma + 1, it.hi});
@@ -235,6 +239,167 @@ void build_lbvh(uint32_t n, const float* v, Lbvh& b) {
                 }
             }
         }
+    }
+}
+
+// ------------------------------------------------------------------------------ 8-wide collapse
+
+// Directed roundings of FP32 operations, exact for all finite inputs: the rounding error
+// of a - b comes from TwoSum, that of x / 255 from an FMA remainder.
+inline float sub_round(float a, float b, bool up) {
+    const float s = a - b;
+    const float bb = s - a;
+    const float e = (a - (s - bb)) + (-b - bb);  // a - b = s + e exactly
+    if (up && e > 0.0f) return std::nextafter(s, std::numeric_limits<float>::infinity());
+    if (!up && e < 0.0f) return std::nextafter(s, -std::numeric_limits<float>::infinity());
+    return s;
+}
+
+inline float div255_up(float x) {
+    const float q = x / 255.0f;
+    const float r = std::fma(-q, 255.0f, x);  // x - 255 q exactly
+    return r > 0.0f ? std::nextafter(q, std::numeric_limits<float>::infinity()) : q;
+}
+
+struct WideEntryO {
+    int ref, first, size;
+    float lo[3], hi[3];
+};
+
+inline float half_area_o(const float lo[3], const float hi[3]) {
+    const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+    return (dx * dy + dy * dz) + dz * dx;
+}
+
+// 8-wide record of every internal node of b, 24 words each, restating k_collapse8
+// (quasi_gb300/csrc/bvh.cu): greedy opening of the largest child by surface area, leaves of
+// one triangle, child boxes on an 8-bit power-of-two grid rounded
+// outwards, children placed in slots by direction (Ylitie, Karras and Laine 2017).
+void collapse8(const Lbvh& b, std::vector<uint32_t>& out) {
+    const uint32_t nodes = b.n > 1 ? b.n - 1 : (b.n == 1 ? 1 : 0);
+    out.assign(24ull * nodes, 0u);
+    auto entry = [&](int c, int k, WideEntryO& e) {
+        e.ref = b.child[2ull * c + k];
+        const float* bx = &b.box[12ull * c + 6 * k];
+        for (int a = 0; a < 3; ++a) {
+            e.lo[a] = bx[a];
+            e.hi[a] = bx[3 + a];
+        }
+        if (e.ref < 0) {
+            e.first = ~e.ref;
+            e.size = 1;
+        } else {
+            e.first = b.range[2ull * e.ref];
+            e.size = b.range[2ull * e.ref + 1] - e.first + 1;
+        }
+    };
+    for (uint32_t nb = 0; nb < nodes; ++nb) {
+        WideEntryO e[8];
+        entry(static_cast<int>(nb), 0, e[0]);
+        entry(static_cast<int>(nb), 1, e[1]);
+        int count = 2;
+        while (count < 8) {
+            int pick = -1;
+            float best = 0.0f;
+            for (int i = 0; i < count; ++i) {
+                if (e[i].ref < 0) continue;
+                const float a = half_area_o(e[i].lo, e[i].hi);
+                if (pick < 0 || a > best) {
+                    pick = i;
+                    best = a;
+                }
+            }
+            if (pick < 0) break;
+            const int c = e[pick].ref;
+            entry(c, 1, e[count]);
+            entry(c, 0, e[pick]);
+            ++count;
+        }
+        float lo[3], hi[3];
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = e[0].lo[a];
+            hi[a] = e[0].hi[a];
+            for (int i = 1; i < count; ++i) {
+                lo[a] = std::fmin(lo[a], e[i].lo[a]);
+                hi[a] = std::fmax(hi[a], e[i].hi[a]);
+            }
+        }
+        uint32_t ex[3];
+        double inv_s[3];
+        for (int a = 0; a < 3; ++a) {
+            const float x = div255_up(sub_round(hi[a], lo[a], true));
+            uint32_t bits;
+            std::memcpy(&bits, &x, 4);
+            const int eb = static_cast<int>((bits >> 23) & 0xffu);
+            int ee = eb == 0 ? -100 : eb - 127 + ((bits & 0x7fffffu) != 0u ? 1 : 0);
+            ee = std::max(-100, std::min(126, ee));
+            ex[a] = static_cast<uint32_t>(ee + 127);
+            inv_s[a] = std::ldexp(1.0, -ee);
+        }
+        const float mx = (lo[0] + hi[0]) * 0.5f, my = (lo[1] + hi[1]) * 0.5f, mz = (lo[2] + hi[2]) * 0.5f;
+        float cx[8], cy[8], cz[8];
+        for (int i = 0; i < count; ++i) {
+            cx[i] = (e[i].lo[0] + e[i].hi[0]) * 0.5f - mx;
+            cy[i] = (e[i].lo[1] + e[i].hi[1]) * 0.5f - my;
+            cz[i] = (e[i].lo[2] + e[i].hi[2]) * 0.5f - mz;
+        }
+        int slot_of[8] = {};
+        uint32_t used = 0, placed = 0;
+        for (int it = 0; it < count; ++it) {
+            int bi = -1, bs = -1;
+            float bsc = 0.0f;
+            for (int i = 0; i < count; ++i) {
+                if (placed & (1u << i)) continue;
+                for (int s = 0; s < 8; ++s) {
+                    if (used & (1u << s)) continue;
+                    const float sc = (((s & 1) ? -cx[i] : cx[i]) + ((s & 2) ? -cy[i] : cy[i])) + ((s & 4) ? -cz[i] : cz[i]);
+                    if (bi < 0 || sc > bsc) {
+                        bi = i;
+                        bs = s;
+                        bsc = sc;
+                    }
+                }
+            }
+            slot_of[bi] = bs;
+            placed |= 1u << bi;
+            used |= 1u << bs;
+        }
+        uint32_t* w = &out[24ull * nb];
+        uint32_t qlo[3][2] = {}, qhi[3][2] = {};
+        int32_t refs[8];
+        uint32_t imask = 0;
+        for (int s = 0; s < 8; ++s) {
+            refs[s] = ~3;
+            for (int a = 0; a < 3; ++a) qlo[a][s >> 2] |= 255u << (8 * (s & 3));
+        }
+        for (int i = 0; i < count; ++i) {
+            const int s = slot_of[i];
+            for (int a = 0; a < 3; ++a) {
+                const double ql = std::floor(double(sub_round(e[i].lo[a], lo[a], false)) * inv_s[a]);
+                const double qh = std::ceil(double(sub_round(e[i].hi[a], lo[a], true)) * inv_s[a]);
+                const uint32_t bl = static_cast<uint32_t>(std::min(std::max(ql, 0.0), 255.0));
+                const uint32_t bh = static_cast<uint32_t>(std::min(std::max(qh, 0.0), 255.0));
+                qlo[a][s >> 2] = (qlo[a][s >> 2] & ~(255u << (8 * (s & 3)))) | (bl << (8 * (s & 3)));
+                qhi[a][s >> 2] |= bh << (8 * (s & 3));
+            }
+            if (e[i].ref >= 0 && e[i].size > 1) {  // leaves of one triangle (k_wide_leaf_max)
+                refs[s] = e[i].ref;
+                imask |= 1u << s;
+            } else {
+                refs[s] = ~((e[i].first << 2) | (e[i].size - 1));
+            }
+        }
+        std::memcpy(&w[0], &lo[0], 4);
+        std::memcpy(&w[1], &lo[1], 4);
+        std::memcpy(&w[2], &lo[2], 4);
+        w[3] = ex[0] | (ex[1] << 8) | (ex[2] << 16) | (imask << 24);
+        for (int a = 0; a < 3; ++a) {
+            w[4 + 4 * a] = qlo[a][0];
+            w[5 + 4 * a] = qlo[a][1];
+            w[6 + 4 * a] = qhi[a][0];
+            w[7 + 4 * a] = qhi[a][1];
+        }
+        for (int s = 0; s < 8; ++s) std::memcpy(&w[16 + s], &refs[s], 4);
     }
 }
 
@@ -680,6 +845,15 @@ ORACLE_API int oracle_intersect_quad(const double* ro, const double* rd, const f
     p[0] = pp.x; p[1] = pp.y; p[2] = pp.z;
     n[0] = nn.x; n[1] = nn.y; n[2] = nn.z;
     return 1;
+}
+
+ORACLE_API int oracle_collapse8(uint32_t n, const float* v, uint32_t* words) {
+    Lbvh b;
+    build_lbvh(n, v, b);
+    std::vector<uint32_t> w;
+    collapse8(b, w);
+    if (words && !w.empty()) std::memcpy(words, w.data(), sizeof(uint32_t) * w.size());
+    return 0;
 }
 
 ORACLE_API int oracle_lbvh(uint32_t n, const float* v, uint32_t* morton, uint32_t* order, int32_t* children,

@@ -50,6 +50,8 @@ def lib() -> C.CDLL:
         L.oracle_intersect_quad.argtypes = [P, P, P, C.c_double, C.c_double, P, P, P]
         L.oracle_lbvh.restype = C.c_int
         L.oracle_lbvh.argtypes = [C.c_uint32, P, P, P, P, P, P]
+        L.oracle_collapse8.restype = C.c_int
+        L.oracle_collapse8.argtypes = [C.c_uint32, P, P]
         L.oracle_render_nee.restype = C.c_int
         L.oracle_render_nee.argtypes = [C.c_uint32, P, P, P, C.POINTER(OracleConfig), P, C.c_uint32, P, P, P, P, P]
         L.oracle_render_reference.restype = C.c_int
@@ -131,6 +133,33 @@ def lbvh(vertices: np.ndarray) -> dict[str, np.ndarray]:
     if rc:
         raise RuntimeError(f"oracle_lbvh failed: {rc}")
     return out
+
+
+def collapse8(vertices: np.ndarray) -> np.ndarray:
+    """8-wide traversal records of the LBVH, (max(n - 1, 1), 24) uint32 (n = 0: empty)."""
+    v = _f32(vertices).reshape(-1, 9)
+    n = v.shape[0]
+    out = np.zeros((max(n - 1, 1) if n else 0, 24), np.uint32)
+    rc = lib().oracle_collapse8(n, v.ctypes.data, out.ctypes.data)
+    if rc:
+        raise RuntimeError(f"oracle_collapse8 failed: {rc}")
+    return out
+
+
+def wide_reachable(words: np.ndarray) -> list[int]:
+    """Indices of the 8-wide records reachable from record 0 through internal references."""
+    if words.shape[0] == 0:
+        return []
+    refs = words[:, 16:24].view(np.int32)
+    imask = words[:, 3] >> 24
+    seen, todo = [], [0]
+    while todo:
+        i = todo.pop()
+        seen.append(i)
+        for s in range(8):
+            if (int(imask[i]) >> s) & 1:
+                todo.append(int(refs[i, s]))
+    return sorted(seen)
 
 
 def _config(width, height, spp, depth, seed, camera, precision, threads, sample_base, eps) -> OracleConfig:

@@ -92,7 +92,8 @@ class Q_cuda_options(C.Structure):
                 ("integrator", C.c_uint32), ("rebuild_each_frame", C.c_uint32), ("wave_spp", C.c_uint32),
                 ("trace_block", C.c_uint32), ("record_samples", C.c_uint32), ("collect_stats", C.c_uint32),
                 ("profile", C.c_uint32), ("megakernel", C.c_uint32), ("smem_levels", C.c_uint32),
-                ("ray_eps", C.c_float), ("refill_lanes", C.c_uint32), ("trace_steps", C.c_uint32)]
+                ("ray_eps", C.c_float), ("refill_lanes", C.c_uint32), ("trace_steps", C.c_uint32),
+                ("bvh_width", C.c_uint32)]
 
 
 class Q_cuda_stats(C.Structure):
@@ -119,7 +120,8 @@ class Q_cuda_batch_scene(C.Structure):
 class Q_cuda_batch_options(C.Structure):
     _fields_ = [("max_depth", C.c_uint32), ("seed", C.c_uint32), ("form", C.c_uint32), ("wave_paths", C.c_uint32),
                 ("trace_block", C.c_uint32), ("fetch_rays", C.c_uint32), ("use_graph", C.c_uint32),
-                ("collect_stats", C.c_uint32), ("ray_eps", C.c_float)]
+                ("collect_stats", C.c_uint32), ("ray_eps", C.c_float), ("bvh_width", C.c_uint32),
+                ("refill_lanes", C.c_uint32)]
 
 
 class Q_cuda_batch_stats(C.Structure):
@@ -166,6 +168,7 @@ CUDA_SYMBOLS = {
                                       C.POINTER(C.c_uint32)]),
     "Q_cuda_last_error": (C.c_char_p, [C.c_void_p]),
     "Q_cuda_read_bvh": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "Q_cuda_read_wide_bvh": (C.c_int, [C.c_void_p, C.c_void_p]),
     "Q_cuda_read_samples": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "Q_cuda_resolve_device": (C.c_int, [C.c_void_p, C.c_void_p]),
     "Q_cuda_radix_sort_pairs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]),

@@ -25,6 +25,8 @@ CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_FLAGS = ["-O2", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", "-Wall", "-Wextra"]
+# Extra nvcc flags (e.g. -D tuning constants); objects are not rebuilt when only these change.
+EXTRA_NVCC = os.environ.get("QUASI_NVCC_FLAGS", "").split()
 
 
 def _cuda_lib_dir() -> Path:
@@ -60,7 +62,7 @@ def compile_objects(verbose_ptxas: bool = False) -> list[Path]:
     for src in sorted(CSRC.glob("*.cu")):
         obj = BUILD / (src.stem + ".cu.o")
         cmd = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", ",".join(HOST_FLAGS),
-               "--expt-relaxed-constexpr", "-I", str(ROOT / "include"), "-c", str(src), "-o", str(obj)]
+               "--expt-relaxed-constexpr", "-I", str(ROOT / "include"), *EXTRA_NVCC, "-c", str(src), "-o", str(obj)]
         if verbose_ptxas:
             cmd.insert(1, "-Xptxas=-v")
         jobs.append((obj, [src, *headers], cmd))

@@ -68,6 +68,10 @@ int BatchRenderer::validate(Q_cuda_batch_options& o) const {
     if (o.use_graph > 2) return QUASI_ERR_INVALID;
     if (o.wave_paths > k_max_wave_paths) return QUASI_ERR_INVALID;
     if (!(o.ray_eps > 0.f)) o.ray_eps = 1e-4f;
+    if (o.bvh_width == 0) o.bvh_width = 8;
+    if (o.bvh_width != 2 && o.bvh_width != 8) return QUASI_ERR_INVALID;
+    if (o.refill_lanes == 0) o.refill_lanes = k_wide_refill_lanes;
+    if (o.refill_lanes > 32) return QUASI_ERR_INVALID;
     return QUASI_OK;
 }
 
@@ -200,7 +204,8 @@ int BatchRenderer::upload_table() {
                        k_refill_lanes,
                        k_trace_steps,
                        nullptr,
-                       0};
+                       0,
+                       opt_.bvh_width == 2 ? nullptr : bv.wide};
         d.px_offset = h.px_offset;
         d.tri_offset = h.tri_offset;
         d.spp = h.spp;
@@ -282,8 +287,11 @@ int BatchRenderer::ensure_buffers() {
 // Grid sizes of the persistent kernels for the current block sizes: SMs x resident blocks.
 void BatchRenderer::compute_grids() {
     const bool stats = opt_.collect_stats != 0;
-    auto kc = stats ? k_batch_trace_closest<true> : k_batch_trace_closest<false>;
-    auto ks = stats ? k_batch_trace_shadow<true> : k_batch_trace_shadow<false>;
+    const bool wide = opt_.bvh_width != 2;
+    auto kc = stats ? (wide ? k_batch_trace_closest<true, true> : k_batch_trace_closest<true, false>)
+                    : (wide ? k_batch_trace_closest<false, true> : k_batch_trace_closest<false, false>);
+    auto ks = stats ? (wide ? k_batch_trace_shadow<true, true> : k_batch_trace_shadow<true, false>)
+                    : (wide ? k_batch_trace_shadow<false, true> : k_batch_trace_shadow<false, false>);
     auto km = stats ? k_batch_megakernel<true> : k_batch_megakernel<false>;
     const int tb = static_cast<int>(opt_.trace_block), mb = std::min(tb, 128);
     int occ_c = 0, occ_s = 0, occ_m = 0, occ_a = 0;
@@ -314,11 +322,15 @@ int BatchRenderer::record_frame(cudaStream_t s, uint32_t& launches) {
     const int tb = static_cast<int>(opt_.trace_block);
     const int mb = std::min(tb, 128);
     const int chunk = static_cast<int>(opt_.fetch_rays);
+    const int refill = static_cast<int>(opt_.refill_lanes);
     const size_t per_wave = 4ull * D;
     B_TRY(cudaMemsetAsync(counters_.ptr, 0, sizeof(int) * per_wave * std::max<size_t>(waves_.size(), 1), s), "memset");
     const bool stats = opt_.collect_stats != 0;
-    auto kc = stats ? k_batch_trace_closest<true> : k_batch_trace_closest<false>;
-    auto ks = stats ? k_batch_trace_shadow<true> : k_batch_trace_shadow<false>;
+    const bool wide = opt_.bvh_width != 2;
+    auto kc = stats ? (wide ? k_batch_trace_closest<true, true> : k_batch_trace_closest<true, false>)
+                    : (wide ? k_batch_trace_closest<false, true> : k_batch_trace_closest<false, false>);
+    auto ks = stats ? (wide ? k_batch_trace_shadow<true, true> : k_batch_trace_shadow<true, false>)
+                    : (wide ? k_batch_trace_shadow<false, true> : k_batch_trace_shadow<false, false>);
     auto km = stats ? k_batch_megakernel<true> : k_batch_megakernel<false>;
     const int grid_c = grid_c_, grid_s = grid_s_, grid_m = grid_m_;
     const int grid_shade = sm * 8;
@@ -347,7 +359,7 @@ int BatchRenderer::record_frame(cudaStream_t s, uint32_t& launches) {
                 int* f_shadow = cnt + 3 * D + (k - 1);
                 B_TRY(QUASI_LAUNCH(prof_, "batch_trace_closest", s,
                                    (kc<<<grid_c, tb, 0, s>>>(table, meta, qcur, hits_.as<float4>(), c_cur, cap, chunk,
-                                                             f_cur, err, st))),
+                                                             refill, f_cur, err, st))),
                       "batch_trace_closest");
                 B_TRY(QUASI_LAUNCH(prof_, "batch_shade", s,
                                    (k_batch_shade<<<grid_shade, 256, 0, s>>>(table, meta, pd, k, qcur, hits_.as<float4>(),
@@ -356,7 +368,7 @@ int BatchRenderer::record_frame(cudaStream_t s, uint32_t& launches) {
                       "batch_shade");
                 B_TRY(QUASI_LAUNCH(prof_, "batch_trace_shadow", s,
                                    (ks<<<grid_s, tb, 0, s>>>(table, meta, pd, shadow_.as<float4>(), c_shadow, cap, chunk,
-                                                             f_shadow, err, st))),
+                                                             refill, f_shadow, err, st))),
                       "batch_trace_shadow");
             }
         }
@@ -642,7 +654,8 @@ int BatchRenderer::time_frame(float& ms) {
     return QUASI_OK;
 }
 
-// Coordinate search over form, wave size, block size and fetch size on 1-spp frames.
+// Coordinate search over form, wave size, block size and fetch size (warp chunks over the
+// binary LBVH) or refill threshold (8-wide records) on 1-spp frames.
 int BatchRenderer::autotune(double budget_ms, Q_cuda_batch_options* chosen) {
     if (budget_ms <= 0.0) budget_ms = 5000.0;
     const auto t0 = std::chrono::steady_clock::now();
@@ -664,12 +677,18 @@ int BatchRenderer::autotune(double budget_ms, Q_cuda_batch_options* chosen) {
     const uint32_t waves[] = {2u << 20, 4u << 20, 8u << 20, 16u << 20};
     const uint32_t blocks[] = {64, 128, 256};
     const uint32_t fetches[] = {32, 64, 128};
+    const uint32_t refills[] = {4, 8, 16};
+    const bool wide = opt_.bvh_width != 2;
     for (int dim = 0; dim < 4 && elapsed() < budget_ms; ++dim) {
-        const uint32_t* vals = dim == 0 ? forms : dim == 1 ? waves : dim == 2 ? blocks : fetches;
+        const uint32_t* vals = dim == 0 ? forms : dim == 1 ? waves : dim == 2 ? blocks : wide ? refills : fetches;
         const int nv = dim == 0 ? 2 : dim == 1 ? 4 : 3;
         for (int v = 0; v < nv && elapsed() < budget_ms; ++v) {
             Q_cuda_batch_options o = best;
-            uint32_t& field = dim == 0 ? o.form : dim == 1 ? o.wave_paths : dim == 2 ? o.trace_block : o.fetch_rays;
+            uint32_t& field = dim == 0   ? o.form
+                              : dim == 1 ? o.wave_paths
+                              : dim == 2 ? o.trace_block
+                              : wide     ? o.refill_lanes
+                                         : o.fetch_rays;
             const uint32_t cur = dim == 1 && field == 0 ? k_default_wave_paths : field;
             if (vals[v] == cur) continue;
             if (dim == 1 && vals[v] < max_slots_) continue;

@@ -105,42 +105,102 @@ __device__ __forceinline__ void trace_batches_multi(Job& job, const BatchSceneDe
                 TraceState st;
                 st.r = make_ray(o, d);
                 st.tmax = tmax;
-                st.best = trace_bvh<ANY, STATS, false>(s.nodes, s.tris, s.n_tris, st.r, tmax, exclude, st.best_t, st.bu,
-                                                       st.bv, err, cnt);
+                st.best = trace_bvh<ANY, STATS>(s.nodes, s.tris, s.n_tris, st.r, tmax, exclude, st.best_t, st.bu, st.bv,
+                                                err, cnt);
                 job.store(i, st);
             }
         }
     }
 }
 
-template <bool STATS>
+// Persistent traversal over rays of several scenes with per-lane refill on the 8-wide
+// records: once `refill` lanes of a warp are idle they take the next rays with one atomic;
+// each lane traverses the records of its own ray's scene.
+template <bool ANY, bool STATS, class Job>
+__device__ __forceinline__ void trace_wide_refill_multi(Job& job, const BatchSceneDev* __restrict__ scenes,
+                                                        const uint2* __restrict__ meta, int n, int refill,
+                                                        int* __restrict__ fetch, uint32_t& err, TraceCounters& cnt) {
+    const int lane = threadIdx.x & 31;
+    WideRay q;
+    int2 stack[k_wide_stack];
+    const float4* wide = nullptr;
+    const float4* tris = nullptr;
+    bool active = false, exhausted = false;
+    int idx = 0;
+    while (true) {
+        const uint32_t idle = __ballot_sync(0xffffffffu, !active);
+        if (!exhausted && __popc(idle) >= refill) {
+            const int leader = __ffs(idle) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(fetch, __popc(idle));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            exhausted = base + __popc(idle) >= n;
+            if (!active) {
+                idx = base + __popc(idle & lanemask_lt());
+                if (idx < n) {
+                    const SceneDev& s = scenes[meta[job.pid(idx)].x].s;
+                    wide = s.wide;
+                    tris = s.tris;
+                    float3 o, d;
+                    float tmax;
+                    int exclude;
+                    job.load(idx, o, d, tmax, exclude);
+                    wide_begin(q, o, d, tmax, exclude, s.n_tris);
+                    active = true;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) break;
+        if (active && wide_visit<ANY, STATS>(wide, tris, q, stack, err, cnt)) {
+            TraceState st;
+            st.r = q.r;
+            st.tmax = q.tmax;
+            st.best_t = q.best_t;
+            st.best = q.best;
+            st.bu = q.bu;
+            st.bv = q.bv;
+            job.store(idx, st);
+            active = false;
+        }
+    }
+}
+
+// WIDE: per-lane refill over the 8-wide records (refill = idle lanes that trigger a fetch);
+// otherwise warp chunks over the scenes' binary LBVHs.
+template <bool STATS, bool WIDE>
 __global__ void __launch_bounds__(256) k_batch_trace_closest(const BatchSceneDev* __restrict__ scenes,
                                                              const uint2* __restrict__ meta, const float4* __restrict__ q,
                                                              float4* __restrict__ hits, const int* __restrict__ count,
-                                                             int capacity, int chunk, int* __restrict__ fetch,
+                                                             int capacity, int chunk, int refill, int* __restrict__ fetch,
                                                              uint32_t* __restrict__ err,
                                                              unsigned long long* __restrict__ stats) {
     const int n = min(*count, capacity);
     uint32_t e = 0;
     TraceCounters c;
     ClosestJob job{q, hits};
-    trace_batches_multi<false, STATS>(job, scenes, meta, n, chunk, fetch, e, c);
+    if (WIDE)
+        trace_wide_refill_multi<false, STATS>(job, scenes, meta, n, refill, fetch, e, c);
+    else
+        trace_batches_multi<false, STATS>(job, scenes, meta, n, chunk, fetch, e, c);
     if (e) atomicOr(err, e);
     flush_counters<STATS>(c, stats);
 }
 
-template <bool STATS>
+template <bool STATS, bool WIDE>
 __global__ void __launch_bounds__(256) k_batch_trace_shadow(const BatchSceneDev* __restrict__ scenes,
                                                             const uint2* __restrict__ meta, PathDev p,
                                                             const float4* __restrict__ sq, const int* __restrict__ count,
-                                                            int capacity, int chunk, int* __restrict__ fetch,
-                                                            uint32_t* __restrict__ err,
+                                                            int capacity, int chunk, int refill,
+                                                            int* __restrict__ fetch, uint32_t* __restrict__ err,
                                                             unsigned long long* __restrict__ stats) {
     const int n = min(*count, capacity);
     uint32_t e = 0;
     TraceCounters c;
     ShadowJob job{sq, p};
-    trace_batches_multi<true, STATS>(job, scenes, meta, n, chunk, fetch, e, c);
+    if (WIDE)
+        trace_wide_refill_multi<true, STATS>(job, scenes, meta, n, refill, fetch, e, c);
+    else
+        trace_batches_multi<true, STATS>(job, scenes, meta, n, chunk, fetch, e, c);
     if (e) atomicOr(err, e);
     flush_counters<STATS>(c, stats + 2);
 }

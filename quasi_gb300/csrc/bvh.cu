@@ -4,6 +4,7 @@
 // Morton codes, the sort order and the topology bit-exact against the oracle.
 #include "bvh.cuh"
 #include "common.cuh"
+#include "wide.cuh"
 
 #include <algorithm>
 #include <cfloat>
@@ -257,7 +258,9 @@ __global__ void __launch_bounds__(256) k_karras(const uint32_t* __restrict__ key
     const int gamma = i + s * d + min(d, 0);
     const int left = (min(i, j) == gamma) ? ~gamma : gamma;
     const int right = (max(i, j) == gamma + 1) ? ~(gamma + 1) : gamma + 1;
-    nodes[4 * i + 3] = make_float4(__int_as_float(left), __int_as_float(right), 0.f, 0.f);
+    // n3 = (left, right, first leaf, last leaf): the node covers leaves min(i, j) .. max(i, j)
+    nodes[4 * i + 3] = make_float4(__int_as_float(left), __int_as_float(right), __int_as_float(min(i, j)),
+                                   __int_as_float(max(i, j)));
     parent[left >= 0 ? left : (n - 1) + ~left] = i;
     parent[right >= 0 ? right : (n - 1) + ~right] = i;
     if (i == 0) parent[0] = -1;
@@ -284,7 +287,7 @@ __global__ void __launch_bounds__(256) k_leaf_boxes(const float4* __restrict__ t
         nodes[0] = make_float4(lo.x, hi.x, lo.y, hi.y);
         nodes[1] = make_float4(lo.x, hi.x, lo.y, hi.y);
         nodes[2] = make_float4(lo.z, hi.z, lo.z, hi.z);
-        nodes[3] = make_float4(__int_as_float(~0), __int_as_float(~0), 0.f, 0.f);
+        nodes[3] = make_float4(__int_as_float(~0), __int_as_float(~0), __int_as_float(0), __int_as_float(0));
         return;
     }
     int child = ~i;
@@ -312,6 +315,162 @@ __global__ void __launch_bounds__(256) k_leaf_boxes(const float4* __restrict__ t
         child = p;
         p = parent[p];
     }
+}
+
+// ---------------------------------------------------------------- 8-wide collapse (wide.cuh)
+
+struct WideEntry {
+    int ref;     // binary child: >= 0 internal node, < 0 leaf ~pos
+    int first;   // first leaf of the subtree
+    int size;    // leaves in the subtree
+    float lo[3], hi[3];
+};
+
+__device__ __forceinline__ float half_area(const float lo[3], const float hi[3]) {
+    const float dx = __fsub_rn(hi[0], lo[0]), dy = __fsub_rn(hi[1], lo[1]), dz = __fsub_rn(hi[2], lo[2]);
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dy), __fmul_rn(dy, dz)), __fmul_rn(dz, dx));
+}
+
+// Child k (0/1) of binary node c as a collapse entry; reads c's record (and, for an internal
+// child, that child's leaf range).
+__device__ __forceinline__ void wide_entry(const float4* __restrict__ nodes, int c, int k, WideEntry& e) {
+    const float4 nb = __ldg(&nodes[4 * c + k]);
+    const float4 n2 = __ldg(&nodes[4 * c + 2]);
+    const float4 n3 = __ldg(&nodes[4 * c + 3]);
+    e.ref = __float_as_int(k == 0 ? n3.x : n3.y);
+    e.lo[0] = nb.x;
+    e.hi[0] = nb.y;
+    e.lo[1] = nb.z;
+    e.hi[1] = nb.w;
+    e.lo[2] = k == 0 ? n2.x : n2.z;
+    e.hi[2] = k == 0 ? n2.y : n2.w;
+    if (e.ref < 0) {
+        e.first = ~e.ref;
+        e.size = 1;
+    } else {
+        const float4 m3 = __ldg(&nodes[4 * e.ref + 3]);
+        e.first = __float_as_int(m3.z);
+        e.size = __float_as_int(m3.w) - e.first + 1;
+    }
+}
+
+// Smallest e (clamped to [-100, 126]) with 255 * 2^e >= hi - lo, as the biased exponent byte.
+__device__ __forceinline__ uint32_t wide_exponent(float lo, float hi) {
+    const float x = __fdiv_ru(__fsub_ru(hi, lo), 255.0f);
+    const uint32_t bits = __float_as_uint(x);
+    const int ebits = static_cast<int>((bits >> 23) & 0xffu);
+    int e = ebits == 0 ? -100 : ebits - 127 + ((bits & 0x7fffffu) != 0u ? 1 : 0);
+    e = max(-100, min(126, e));
+    return static_cast<uint32_t>(e + 127);
+}
+
+// One thread per binary internal node b: the wide record of b's subtree (layout in wide.cuh).
+__global__ void __launch_bounds__(128) k_collapse8(const float4* __restrict__ nodes, int n_internal,
+                                                   float4* __restrict__ wide) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n_internal) return;
+    WideEntry e[8];
+    wide_entry(nodes, b, 0, e[0]);
+    wide_entry(nodes, b, 1, e[1]);
+    int count = 2;
+    // greedy opening: the internal child of largest surface area, ties to the lower entry
+    while (count < 8) {
+        int pick = -1;
+        float best = 0.0f;
+        for (int i = 0; i < count; ++i) {
+            if (e[i].ref < 0) continue;
+            const float a = half_area(e[i].lo, e[i].hi);
+            if (pick < 0 || a > best) {
+                pick = i;
+                best = a;
+            }
+        }
+        if (pick < 0) break;
+        const int c = e[pick].ref;
+        wide_entry(nodes, c, 1, e[count]);
+        wide_entry(nodes, c, 0, e[pick]);
+        ++count;
+    }
+    // node box, grid origin and scale
+    float lo[3], hi[3];
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = e[0].lo[a];
+        hi[a] = e[0].hi[a];
+        for (int i = 1; i < count; ++i) {
+            lo[a] = fminf(lo[a], e[i].lo[a]);
+            hi[a] = fmaxf(hi[a], e[i].hi[a]);
+        }
+    }
+    uint32_t ex[3];
+    float inv_s[3];
+    for (int a = 0; a < 3; ++a) {
+        ex[a] = wide_exponent(lo[a], hi[a]);
+        inv_s[a] = __uint_as_float((254u - ex[a]) << 23);  // 2^-e for e in [-100, 126]
+    }
+    // slots by direction: child i goes to the free slot s maximising sum_a sign_s(a) * c_i(a),
+    // c_i = child centre - node centre, sign negative where bit a of s is set; greedy over
+    // (child, slot) pairs in descending score, ties to the lower child, then the lower slot
+    float cx[8], cy[8], cz[8];
+    const float mx = __fmul_rn(__fadd_rn(lo[0], hi[0]), 0.5f), my = __fmul_rn(__fadd_rn(lo[1], hi[1]), 0.5f),
+                mz = __fmul_rn(__fadd_rn(lo[2], hi[2]), 0.5f);
+    for (int i = 0; i < count; ++i) {
+        cx[i] = __fsub_rn(__fmul_rn(__fadd_rn(e[i].lo[0], e[i].hi[0]), 0.5f), mx);
+        cy[i] = __fsub_rn(__fmul_rn(__fadd_rn(e[i].lo[1], e[i].hi[1]), 0.5f), my);
+        cz[i] = __fsub_rn(__fmul_rn(__fadd_rn(e[i].lo[2], e[i].hi[2]), 0.5f), mz);
+    }
+    int slot_of[8];
+    uint32_t used_slots = 0, placed = 0;
+    for (int it = 0; it < count; ++it) {
+        int bi = -1, bs = -1;
+        float bsc = 0.0f;
+        for (int i = 0; i < count; ++i) {
+            if (placed & (1u << i)) continue;
+            for (int s = 0; s < 8; ++s) {
+                if (used_slots & (1u << s)) continue;
+                const float sc = __fadd_rn(__fadd_rn((s & 1) ? -cx[i] : cx[i], (s & 2) ? -cy[i] : cy[i]),
+                                           (s & 4) ? -cz[i] : cz[i]);
+                if (bi < 0 || sc > bsc) {
+                    bi = i;
+                    bs = s;
+                    bsc = sc;
+                }
+            }
+        }
+        slot_of[bi] = bs;
+        placed |= 1u << bi;
+        used_slots |= 1u << bs;
+    }
+    uint32_t qb[3][2][2] = {};  // [axis][lo/hi][word]: bytes of slots 0..3 and 4..7
+    int refs[8];
+    uint32_t imask = 0;
+    for (int s = 0; s < 8; ++s) {
+        refs[s] = k_wide_empty_ref;
+        for (int a = 0; a < 3; ++a) qb[a][0][s >> 2] |= 255u << (8 * (s & 3));
+    }
+    for (int i = 0; i < count; ++i) {
+        const int s = slot_of[i];
+        for (int a = 0; a < 3; ++a) {
+            const float ql = floorf(__fmul_rd(__fsub_rd(e[i].lo[a], lo[a]), inv_s[a]));
+            const float qh = ceilf(__fmul_ru(__fsub_ru(e[i].hi[a], lo[a]), inv_s[a]));
+            const uint32_t bl = static_cast<uint32_t>(fminf(fmaxf(ql, 0.0f), 255.0f));
+            const uint32_t bh = static_cast<uint32_t>(fminf(fmaxf(qh, 0.0f), 255.0f));
+            qb[a][0][s >> 2] = (qb[a][0][s >> 2] & ~(255u << (8 * (s & 3)))) | (bl << (8 * (s & 3)));
+            qb[a][1][s >> 2] |= bh << (8 * (s & 3));
+        }
+        if (e[i].ref >= 0 && e[i].size > k_wide_leaf_max) {
+            refs[s] = e[i].ref;
+            imask |= 1u << s;
+        } else {
+            refs[s] = ~((e[i].first << 2) | (e[i].size - 1));
+        }
+    }
+    float4* w = wide + k_wide_node_f4 * static_cast<size_t>(b);
+    w[0] = make_float4(lo[0], lo[1], lo[2], __uint_as_float(ex[0] | (ex[1] << 8) | (ex[2] << 16) | (imask << 24)));
+    for (int a = 0; a < 3; ++a)
+        w[1 + a] = make_float4(__uint_as_float(qb[a][0][0]), __uint_as_float(qb[a][0][1]), __uint_as_float(qb[a][1][0]),
+                               __uint_as_float(qb[a][1][1]));
+    w[4] = make_float4(__int_as_float(refs[0]), __int_as_float(refs[1]), __int_as_float(refs[2]), __int_as_float(refs[3]));
+    w[5] = make_float4(__int_as_float(refs[4]), __int_as_float(refs[5]), __int_as_float(refs[6]), __int_as_float(refs[7]));
 }
 
 // Copies the first `count` internal nodes in breadth-first order (the top levels of the
@@ -426,6 +585,7 @@ cudaError_t LbvhBuilder::reserve(uint32_t n) {
     QUASI_TRY_CUDA(cudaMalloc(&flags_, sizeof(uint32_t) * m));
     QUASI_TRY_CUDA(cudaMalloc(&nodes_, sizeof(float4) * 4 * m));
     QUASI_TRY_CUDA(cudaMalloc(&tris_, sizeof(float4) * 3 * m));
+    QUASI_TRY_CUDA(cudaMalloc(&wide_, sizeof(float4) * k_wide_node_f4 * m));
     QUASI_TRY_CUDA(radix_sort_reserve(sort_, m));
     capacity_ = m;
     return cudaSuccess;
@@ -434,12 +594,13 @@ cudaError_t LbvhBuilder::reserve(uint32_t n) {
 void LbvhBuilder::release() {
     for (void* p : {static_cast<void*>(bounds_), static_cast<void*>(partial_), static_cast<void*>(morton_),
                     static_cast<void*>(keys_), static_cast<void*>(order_), static_cast<void*>(parent_),
-                    static_cast<void*>(flags_), static_cast<void*>(nodes_), static_cast<void*>(tris_)})
+                    static_cast<void*>(flags_), static_cast<void*>(nodes_), static_cast<void*>(tris_),
+                    static_cast<void*>(wide_)})
         if (p) cudaFree(p);
     bounds_ = partial_ = nullptr;
     morton_ = keys_ = order_ = flags_ = nullptr;
     parent_ = nullptr;
-    nodes_ = tris_ = nullptr;
+    nodes_ = tris_ = wide_ = nullptr;
     if (tree_) cudaFree(tree_);
     tree_ = nullptr;
     tree_n_ = tree_capacity_ = 0;
@@ -471,6 +632,10 @@ cudaError_t LbvhBuilder::build(const float4* tri_in, uint32_t n, cudaStream_t st
     QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_leaf_boxes", stream,
                                 (k_leaf_boxes<<<ceil_div(n, 256), 256, 0, stream>>>(
                                     tri_in, order_, static_cast<int>(n), parent_, nodes_, flags_, tris_, err))));
+    const uint32_t internal = n > 1 ? n - 1 : 1;
+    QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_collapse8", stream,
+                                (k_collapse8<<<ceil_div(internal, 128), 128, 0, stream>>>(
+                                    nodes_, static_cast<int>(internal), wide_))));
     return cudaSuccess;
 }
 
@@ -501,6 +666,14 @@ cudaError_t LbvhBuilder::read(uint32_t* morton, uint32_t* order, int32_t* childr
             }
         }
     }
+    return cudaSuccess;
+}
+
+cudaError_t LbvhBuilder::read_wide(uint32_t* words, cudaStream_t stream) const {
+    QUASI_TRY_CUDA(cudaStreamSynchronize(stream));
+    if (n_ == 0 || !words) return cudaSuccess;
+    const uint32_t nodes = n_ > 1 ? n_ - 1 : 1;
+    QUASI_TRY_CUDA(cudaMemcpy(words, wide_, sizeof(float4) * k_wide_node_f4 * nodes, cudaMemcpyDeviceToHost));
     return cudaSuccess;
 }
 

@@ -8,12 +8,14 @@
 //   4. Karras 2012 hierarchy (index-augmented common-prefix for duplicate codes)
 //   5. bottom-up child boxes with per-node arrival counters; triangles gathered into
 //      leaf order as {v0, orig index}, {e1}, {e2}
+//   6. the 8-wide traversal records collapsed from the binary nodes (wide.cuh)
 //
 // Node layout, 64 bytes (4 x float4), child boxes stored in the parent:
 //   n0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
 //   n1 = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
 //   n2 = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
-//   n3 = (child0, child1, 0, 0) as ints; child >= 0 internal node, child < 0 leaf ~pos.
+//   n3 = (child0, child1, first, last) as ints; child >= 0 internal node, child < 0 leaf ~pos;
+//        the node covers leaves first .. last (a contiguous Morton range).
 // A scene of one triangle gets a single node whose second child has an empty box.
 #pragma once
 
@@ -47,6 +49,7 @@ struct LbvhView {
     uint32_t node_count = 0;
     const float4* tree = nullptr;   // top levels in breadth-first order (for shared memory)
     int tree_n = 0;                 // nodes in `tree`
+    const float4* wide = nullptr;   // 8-wide records (wide.cuh), one per internal node
 };
 
 class LbvhBuilder {
@@ -67,12 +70,14 @@ public:
     cudaError_t build_treelet(int max_nodes, cudaStream_t stream, KernelProfiler& prof);
 
     LbvhView view() const {
-        return LbvhView{nodes_, tris_, n_, n_ == 0 ? 0u : (n_ > 1 ? n_ - 1 : 1u), tree_, tree_n_};
+        return LbvhView{nodes_, tris_, n_, n_ == 0 ? 0u : (n_ > 1 ? n_ - 1 : 1u), tree_, tree_n_, wide_};
     }
 
     // Debug copies to host (stream-synchronous).
     cudaError_t read(uint32_t* morton, uint32_t* order, int32_t* children, float* boxes,
                      float* bounds, cudaStream_t stream) const;
+    // The 8-wide records as 24 words per internal node (stream-synchronous).
+    cudaError_t read_wide(uint32_t* words, cudaStream_t stream) const;
 
 private:
     uint32_t n_ = 0;
@@ -86,6 +91,7 @@ private:
     uint32_t* flags_ = nullptr;      // arrival counters, n-1
     float4* nodes_ = nullptr;
     float4* tris_ = nullptr;
+    float4* wide_ = nullptr;         // 8-wide records, 96 bytes per internal node
     float4* tree_ = nullptr;
     int tree_n_ = 0;
     int tree_capacity_ = 0;

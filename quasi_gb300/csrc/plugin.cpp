@@ -277,6 +277,12 @@ Q_CUDA_EXPORT int Q_cuda_read_bvh(Q_plugin_handle* handle, uint32_t* morton, uin
     return r->read_bvh(morton, order, children, boxes, bounds);
 }
 
+Q_CUDA_EXPORT int Q_cuda_read_wide_bvh(Q_plugin_handle* handle, uint32_t* words) {
+    Q_STATE_OR_FAIL(handle);
+    if (!words) return QUASI_ERR_INVALID;
+    return r->read_wide_bvh(words);
+}
+
 Q_CUDA_EXPORT int Q_cuda_read_samples(Q_plugin_handle* handle, float* radiance, uint32_t* signatures) {
     Q_STATE_OR_FAIL(handle);
     return r->read_samples(radiance, signatures);

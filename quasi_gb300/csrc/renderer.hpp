@@ -57,6 +57,7 @@ public:
     int resolve_device(float* device_rgba);
     int read_samples(float* radiance, uint32_t* signatures);
     int read_bvh(uint32_t* morton, uint32_t* order, int32_t* children, float* boxes, float* bounds);
+    int read_wide_bvh(uint32_t* words);
     int stats(Q_cuda_stats* out);
     int kernel_times(Q_cuda_kernel_time* out, uint32_t capacity, uint32_t* count);
     int autotune(double budget_ms);

@@ -211,6 +211,8 @@ int Renderer::set_options(const Q_cuda_options& o) {
     if (n.refill_lanes > 32) return fail(QUASI_ERR_INVALID, "refill_lanes must be at most 32");
     if (n.smem_levels > 9 && n.smem_levels != 32)
         return fail(QUASI_ERR_INVALID, "smem_levels must be 0 (default), 1..9, or 32 (none)");
+    if (n.bvh_width != 0 && n.bvh_width != 2 && n.bvh_width != 8)
+        return fail(QUASI_ERR_INVALID, "bvh_width must be 0 (default), 2 or 8");
     const bool changed = n.seed != opt_.seed || n.max_depth != opt_.max_depth || n.integrator != opt_.integrator ||
                          n.ray_eps != opt_.ray_eps;
     opt_ = n;
@@ -341,15 +343,17 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
     if (opt_.collect_stats) R_TRY(cudaMemsetAsync(stats_dev_.ptr, 0, sizeof(unsigned long long) * 4, s), "memset");
 
     const LbvhView bv = bvh_.view();
+    const bool wide = opt_.bvh_width != 2;
     SceneDev sd{tri_in_.as<float4>(), albedo_.as<float4>(), emission_.as<float4>(), emitters_.as<int>(),
                 bv.nodes,
                 bv.tris,
                 n_tris_,
                 n_emit_,
-                opt_.refill_lanes ? static_cast<int>(opt_.refill_lanes) : k_refill_lanes,
+                opt_.refill_lanes ? static_cast<int>(opt_.refill_lanes) : (wide ? k_wide_refill_lanes : k_refill_lanes),
                 opt_.trace_steps ? static_cast<int>(opt_.trace_steps) : k_trace_steps,
-                bv.tree,
-                bv.tree_n};
+                wide ? nullptr : bv.tree,
+                wide ? 0 : bv.tree_n,
+                wide ? bv.wide : nullptr};
     const size_t tree_smem = sizeof(float4) * 4 * static_cast<size_t>(sd.tree_n);
     PathDev pd{beta_.as<float4>(),  lpath_.as<float4>(), aov_a_.as<float4>(),
                aov_n_.as<float4>(), ray_ff_.as<float4>(), opt_.record_samples ? sig_.as<uint32_t>() : nullptr};
@@ -367,17 +371,22 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
     const int tb = opt_.trace_block ? static_cast<int>(opt_.trace_block) : 128;
     using ClosestFn = void (*)(SceneDev, const float4*, float4*, const int*, int, int*, uint32_t*, unsigned long long*);
     using ShadowFn = void (*)(SceneDev, PathDev, const float4*, const int*, int, int*, uint32_t*, unsigned long long*);
-    const int mode = sd.refill < 32 ? k_mode_refill : (sd.tree_n > 0 ? k_mode_batch_tree : k_mode_batch);
-    static const ClosestFn closest_fns[2][3] = {
+    const int mode = wide ? (sd.refill < 32 ? k_mode_wide_refill : k_mode_wide)
+                          : sd.refill < 32 ? k_mode_refill : (sd.tree_n > 0 ? k_mode_batch_tree : k_mode_batch);
+    static const ClosestFn closest_fns[2][5] = {
         {k_trace_closest<false, k_mode_batch>, k_trace_closest<false, k_mode_batch_tree>,
-         k_trace_closest<false, k_mode_refill>},
+         k_trace_closest<false, k_mode_refill>, k_trace_closest<false, k_mode_wide>,
+         k_trace_closest<false, k_mode_wide_refill>},
         {k_trace_closest<true, k_mode_batch>, k_trace_closest<true, k_mode_batch_tree>,
-         k_trace_closest<true, k_mode_refill>}};
-    static const ShadowFn shadow_fns[2][3] = {
+         k_trace_closest<true, k_mode_refill>, k_trace_closest<true, k_mode_wide>,
+         k_trace_closest<true, k_mode_wide_refill>}};
+    static const ShadowFn shadow_fns[2][5] = {
         {k_trace_shadow<false, k_mode_batch>, k_trace_shadow<false, k_mode_batch_tree>,
-         k_trace_shadow<false, k_mode_refill>},
+         k_trace_shadow<false, k_mode_refill>, k_trace_shadow<false, k_mode_wide>,
+         k_trace_shadow<false, k_mode_wide_refill>},
         {k_trace_shadow<true, k_mode_batch>, k_trace_shadow<true, k_mode_batch_tree>,
-         k_trace_shadow<true, k_mode_refill>}};
+         k_trace_shadow<true, k_mode_refill>, k_trace_shadow<true, k_mode_wide>,
+         k_trace_shadow<true, k_mode_wide_refill>}};
     const ClosestFn kc = closest_fns[opt_.collect_stats ? 1 : 0][mode];
     const ShadowFn ks = shadow_fns[opt_.collect_stats ? 1 : 0][mode];
     int occ_c = 0, occ_s = 0;
@@ -439,9 +448,11 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
 }
 
 SceneDev Renderer_scene_dev(const LbvhView& bv, const DeviceBuffer& tri_in, const DeviceBuffer& albedo,
-                            const DeviceBuffer& emission, const DeviceBuffer& emitters, uint32_t n_tris, uint32_t n_emit) {
+                            const DeviceBuffer& emission, const DeviceBuffer& emitters, uint32_t n_tris, uint32_t n_emit,
+                            uint32_t bvh_width) {
     return SceneDev{tri_in.as<float4>(), albedo.as<float4>(), emission.as<float4>(), emitters.as<int>(), bv.nodes,
-                    bv.tris, n_tris, n_emit, k_refill_lanes, k_trace_steps, nullptr, 0};
+                    bv.tris, n_tris, n_emit, k_refill_lanes, k_trace_steps, nullptr, 0,
+                    bvh_width == 2 ? nullptr : bv.wide};
 }
 
 FrameParams Renderer::frame_params(uint32_t spp, uint32_t slots, uint32_t tiles_x) const {
@@ -477,7 +488,8 @@ int Renderer::render_megakernel(cudaStream_t s, uint32_t spp) {
     R_TRY(cudaMemsetAsync(counters_.ptr, 0, sizeof(int) * (waves + 2), s), "memset");
     R_TRY(cudaMemsetAsync(stats_dev_.ptr, 0, sizeof(unsigned long long) * 4, s), "memset");
     R_TRY(cudaMemsetAsync(stats_dev_.as<unsigned long long>() + 5, 0, sizeof(unsigned long long) * 2, s), "memset");
-    const SceneDev sd = Renderer_scene_dev(bvh_.view(), tri_in_, albedo_, emission_, emitters_, n_tris_, n_emit_);
+    const SceneDev sd = Renderer_scene_dev(bvh_.view(), tri_in_, albedo_, emission_, emitters_, n_tris_, n_emit_,
+                                           opt_.bvh_width);
     PathDev pd{beta_.as<float4>(),  lpath_.as<float4>(), aov_a_.as<float4>(),
                aov_n_.as<float4>(), ray_ff_.as<float4>(), opt_.record_samples ? sig_.as<uint32_t>() : nullptr};
     FrameParams f = frame_params(spp, slots, tiles_x);
@@ -548,7 +560,8 @@ int Renderer::backward(const float* grad_image, uint32_t spp, uint32_t sample_ba
     f.wave_spp = spp;
     f.sample_base = sample_base;
     f.wave_offset = 0;
-    const SceneDev sd = Renderer_scene_dev(bvh_.view(), tri_in_, albedo_, emission_, emitters_, n_tris_, n_emit_);
+    const SceneDev sd = Renderer_scene_dev(bvh_.view(), tri_in_, albedo_, emission_, emitters_, n_tris_, n_emit_,
+                                           opt_.bvh_width);
     int occ = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjoint, 128, 0);
     const int grid = sm_count_ * std::max(occ, 1);
@@ -627,6 +640,16 @@ int Renderer::read_bvh(uint32_t* morton, uint32_t* order, int32_t* children, flo
         bvh_dirty_ = false;
     }
     R_TRY(bvh_.read(morton, order, children, boxes, bounds, stream_), "read bvh");
+    return QUASI_OK;
+}
+
+int Renderer::read_wide_bvh(uint32_t* words) {
+    if (!has_scene_) return fail(QUASI_ERR_STATE, "no scene");
+    if (bvh_dirty_) {
+        R_TRY(bvh_.build(tri_in_.as<float4>(), n_tris_, stream_, prof_, err_dev_.as<uint32_t>()), "lbvh build");
+        bvh_dirty_ = false;
+    }
+    R_TRY(bvh_.read_wide(words, stream_), "read wide bvh");
     return QUASI_OK;
 }
 

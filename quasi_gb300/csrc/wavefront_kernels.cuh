@@ -4,7 +4,8 @@
 // One wave = wave_spp samples of every pixel. Per wave:
 //   k_camera          camera rays for every (sample, pixel) -> ray queue
 //   for bounce k = 1..D:
-//     k_trace_closest persistent, warp-fetched closest-hit traversal of the queue (FP32)
+//     k_trace_closest persistent, warp-fetched closest-hit traversal of the queue (FP32),
+//                     over the 8-wide records (wide.cuh) or the binary LBVH nodes
 //     k_shade         emission (k == 1), AOVs (k == 1), light sample -> shadow queue,
 //                     cosine-weighted continuation -> next ray queue; both queues are
 //                     compacted with one atomic per warp (ballot + popc)
@@ -46,9 +47,18 @@ __global__ void __launch_bounds__(256) k_camera(FrameParams f, PathDev p, float4
     }
 }
 
+// Minimum resident 256-thread blocks per SM asked of the compiler for the 8-wide trace
+// kernels, a register cap (4 -> 64 registers per thread). Uncapped, they take 93 registers
+// and 5 blocks of 128 threads fit an SM; at 64 registers (a few bytes of spills) 8 fit, and
+// the 1M-triangle frame renders 18% faster on GB300.
+#ifndef QUASI_WIDE_MIN_BLOCKS
+#define QUASI_WIDE_MIN_BLOCKS 4
+#endif
+constexpr int trace_min_blocks(int mode) { return mode >= k_mode_wide ? QUASI_WIDE_MIN_BLOCKS : 1; }
+
 // Persistent closest-hit traversal.
 template <bool STATS, int MODE>
-__global__ void __launch_bounds__(256) k_trace_closest(SceneDev s, const float4* __restrict__ q,
+__global__ void __launch_bounds__(256, trace_min_blocks(MODE)) k_trace_closest(SceneDev s, const float4* __restrict__ q,
                                                        float4* __restrict__ hits, const int* __restrict__ count,
                                                        int capacity, int* __restrict__ fetch,
                                                        uint32_t* __restrict__ err, unsigned long long* __restrict__ stats) {
@@ -56,7 +66,11 @@ __global__ void __launch_bounds__(256) k_trace_closest(SceneDev s, const float4*
     uint32_t e = 0;
     TraceCounters c;
     ClosestJob job{q, hits};
-    if (MODE == k_mode_refill)
+    if (MODE == k_mode_wide)
+        trace_batches_wide<false, STATS>(job, s.wide, s.tris, s.n_tris, n, fetch, e, c);
+    else if (MODE == k_mode_wide_refill)
+        trace_wide_refill<false, STATS>(job, s.wide, s.tris, s.n_tris, n, s.refill, fetch, e, c);
+    else if (MODE == k_mode_refill)
         trace_persistent<false, STATS>(job, s.nodes, s.tris, s.n_tris, n, s.refill, s.steps, fetch, e, c);
     else if (MODE == k_mode_batch_tree)
         trace_batches<false, STATS, true>(job, s.nodes, s.tris, s.n_tris, n, fetch, e, c, stage_treelet(s), s.tree_n);
@@ -68,7 +82,7 @@ __global__ void __launch_bounds__(256) k_trace_closest(SceneDev s, const float4*
 
 // Persistent any-hit traversal of the shadow queue.
 template <bool STATS, int MODE>
-__global__ void __launch_bounds__(256) k_trace_shadow(SceneDev s, PathDev p, const float4* __restrict__ sq,
+__global__ void __launch_bounds__(256, trace_min_blocks(MODE)) k_trace_shadow(SceneDev s, PathDev p, const float4* __restrict__ sq,
                                                       const int* __restrict__ count, int capacity,
                                                       int* __restrict__ fetch, uint32_t* __restrict__ err,
                                                       unsigned long long* __restrict__ stats) {
@@ -76,7 +90,11 @@ __global__ void __launch_bounds__(256) k_trace_shadow(SceneDev s, PathDev p, con
     uint32_t e = 0;
     TraceCounters c;
     ShadowJob job{sq, p};
-    if (MODE == k_mode_refill)
+    if (MODE == k_mode_wide)
+        trace_batches_wide<true, STATS>(job, s.wide, s.tris, s.n_tris, n, fetch, e, c);
+    else if (MODE == k_mode_wide_refill)
+        trace_wide_refill<true, STATS>(job, s.wide, s.tris, s.n_tris, n, s.refill, fetch, e, c);
+    else if (MODE == k_mode_refill)
         trace_persistent<true, STATS>(job, s.nodes, s.tris, s.n_tris, n, s.refill, s.steps, fetch, e, c);
     else if (MODE == k_mode_batch_tree)
         trace_batches<true, STATS, true>(job, s.nodes, s.tris, s.n_tris, n, fetch, e, c, stage_treelet(s), s.tree_n);

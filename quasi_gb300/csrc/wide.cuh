@@ -1,0 +1,325 @@
+// wide.cuh - 8-wide BVH collapsed from the binary LBVH, and its traversal (FP32).
+//
+// The binary LBVH (bvh.cuh) is the bit-exact structure; this is a derived traversal
+// structure built from it in one kernel (k_collapse8, bvh.cu) after every LBVH build:
+//
+//   * Every binary internal node b gets a wide record at index b, computed from b's subtree
+//     alone: start from b's two children and repeatedly open the internal child of largest
+//     surface area (ties to the lower entry) until 8 children or none left to open.
+//     Children whose subtree holds at most k_wide_leaf_max triangles become leaves: a
+//     leaf is a run of consecutive triangles of the leaf-order array (a binary subtree
+//     covers a contiguous Morton range), so the triangle array is shared with the binary
+//     BVH. Larger internal children refer to their own wide record by binary index.
+//     Only records reachable from record 0 are ever visited; the others are never read.
+//   * Child boxes are quantised to 8 bits per plane on a per-node power-of-two grid with
+//     the lower planes rounded down and the upper planes rounded up, so each decoded box
+//     contains the exact child box (Ylitie, Karras and Laine 2017, "Efficient incoherent
+//     ray traversal on GPUs through compressed wide BVHs").
+//   * Children are placed in slots by direction: slot bit a set means "on the negative
+//     side of axis a" (x = bit 0, y = 1, z = 2). A ray whose direction octant is `oct`
+//     ranks slot s by s ^ oct, so the children it reaches first are taken first.
+//
+// Record layout, 96 bytes (6 x float4):
+//   w0 = (p.x, p.y, p.z, ex | ey << 8 | ez << 16 | imask << 24)
+//        p = grid origin, scale per axis 2^(e - 127), imask = slots holding internal children
+//   w1 = x planes: lo[0..3], lo[4..7], hi[0..3], hi[4..7] (one byte per slot)
+//   w2 = y planes, w3 = z planes (same packing)
+//   w4 = refs[0..3], w5 = refs[4..7]
+//        ref >= 0: internal child, the wide record of binary node `ref`
+//        ref < 0:  leaf, ~ref = pos << 2 | code, triangles pos .. pos + ((code + 1) & 3) - 1
+//                  (code 3 = an empty slot: lo planes 255, hi planes 0, no triangles)
+//
+// Closest hit is the smallest t, and an exact tie goes to the smaller original index, as in
+// the binary traversal (trace.cuh), so both return the same triangle.
+#pragma once
+
+#include "trace.cuh"
+
+namespace quasi {
+
+// Triangles per leaf. Runs of 2-3 triangles save record visits, but the union box of a
+// Morton run is much larger than its triangles' boxes: on the 1M soup they doubled the
+// triangle tests per ray (8.3 vs 3.7 for camera rays), so every leaf holds one triangle.
+constexpr int k_wide_leaf_max = 1;
+constexpr int k_wide_stack = 96;      // (ref, t_near) entries per ray
+constexpr int k_wide_node_f4 = 6;     // float4 per wide record
+constexpr int k_wide_empty_ref = ~3;  // leaf with code 3: no triangles
+// Idle lanes that make a warp of the 8-wide trace kernels fetch new rays (default).
+constexpr int k_wide_refill_lanes = 4;
+
+// Selects a[k] of eight values held in registers (k in 0..7) without local memory.
+template <class T>
+__device__ __forceinline__ T sel8(const T (&a)[8], uint32_t k) {
+    const bool b0 = k & 1u, b1 = k & 2u, b2 = k & 4u;
+    const T c0 = b0 ? a[1] : a[0], c1 = b0 ? a[3] : a[2], c2 = b0 ? a[5] : a[4], c3 = b0 ? a[7] : a[6];
+    const T d0 = b1 ? c1 : c0, d1 = b1 ? c3 : c2;
+    return b2 ? d1 : d0;
+}
+
+// Maps an 8-bit mask in slot space to rank space (bit s -> bit s ^ oct).
+__device__ __forceinline__ uint32_t mask_xor_permute(uint32_t m, uint32_t oct) {
+    if (oct & 1u) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+    if (oct & 2u) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+    if (oct & 4u) m = ((m & 0x0fu) << 4) | ((m >> 4) & 0x0fu);
+    return m;
+}
+
+__device__ __forceinline__ float byte_f(uint32_t w, int k) {
+    return static_cast<float>((w >> (8 * k)) & 0xffu);
+}
+
+// Three-input minimum and maximum (one instruction each on sm_100 and later).
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// Tests the triangles of one leaf; returns true when an any-hit query is done.
+template <bool ANY, bool STATS>
+__device__ __forceinline__ bool wide_leaf(const float4* __restrict__ tris, const RayInv& r, int ref, float tmax,
+                                          int exclude, float& best_t, int& best, float& bu, float& bv,
+                                          TraceCounters& cnt) {
+    const uint32_t x = static_cast<uint32_t>(~ref);
+    const uint32_t pos = x >> 2;
+    const uint32_t count = ((x & 3u) + 1u) & 3u;
+    for (uint32_t j = 0; j < count; ++j) {
+        if (STATS) ++cnt.tris;
+        const float4* t = tris + 3ull * (pos + j);
+        const float4 a = __ldg(t), e1 = __ldg(t + 1), e2 = __ldg(t + 2);
+        const int orig = __float_as_int(a.w);
+        float u, v;
+        const float th = tri_t(r, a, e1, e2, u, v);
+        if (orig != exclude && (th < best_t || (th == best_t && orig < best && th < tmax))) {
+            best_t = th;
+            best = orig;
+            bu = u;
+            bv = v;
+            if (ANY) return true;
+        }
+    }
+    return false;
+}
+
+// Traversal state of one ray over the 8-wide records (the stack lives beside it).
+struct WideRay {
+    RayInv r;
+    uint32_t oct;   // direction octant: bit a set where component a is negative
+    float tmax;
+    int exclude;
+    float best_t;
+    int best;       // original index of the closest hit so far, or -1
+    float bu, bv;
+    int node;       // record to visit next, or -1 when done
+    int sp;
+    uint32_t budget;
+};
+
+__device__ __forceinline__ void wide_begin(WideRay& q, float3 o, float3 d, float tmax, int exclude, uint32_t n_tris) {
+    q.r = make_ray(o, d);
+    // octant from the reciprocals, which carry the sign of a zero component (-0 -> -1e20)
+    q.oct = (q.r.inv.x < 0.0f ? 1u : 0u) | (q.r.inv.y < 0.0f ? 2u : 0u) | (q.r.inv.z < 0.0f ? 4u : 0u);
+    q.tmax = tmax;
+    q.exclude = exclude;
+    q.best_t = tmax;
+    q.best = -1;
+    q.bu = q.bv = 0.0f;
+    q.node = n_tris == 0 ? -1 : 0;
+    q.sp = 0;
+    q.budget = 2u * n_tris + 64u;
+}
+
+// One record visit: tests the 8 child boxes, the triangles of the leaves hit, pushes the
+// internal children hit but the first-ranked, and moves to the next record. Returns true
+// when the traversal has finished (q holds the result).
+template <bool ANY, bool STATS>
+__device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, const float4* __restrict__ tris,
+                                           WideRay& q, int2* stack, uint32_t& err, TraceCounters& cnt) {
+    if (q.node < 0) return true;
+    if (--q.budget == 0u) {
+        err |= k_deverr_traversal;
+        q.node = -1;
+        return true;
+    }
+    if (STATS) ++cnt.nodes;
+    const RayInv& r = q.r;
+    const bool nx = q.oct & 1u, ny = q.oct & 2u, nz = q.oct & 4u;
+    const float4* w = wide + k_wide_node_f4 * static_cast<size_t>(q.node);
+    const float4 w0 = __ldg(w), w1 = __ldg(w + 1), w2 = __ldg(w + 2), w3 = __ldg(w + 3);
+    const int4 w4 = __ldg(reinterpret_cast<const int4*>(w + 4));
+    const int4 w5 = __ldg(reinterpret_cast<const int4*>(w + 5));
+    const uint32_t hdr = __float_as_uint(w0.w);
+    const float sx = __uint_as_float((hdr & 0xffu) << 23);
+    const float sy = __uint_as_float(((hdr >> 8) & 0xffu) << 23);
+    const float sz = __uint_as_float(((hdr >> 16) & 0xffu) << 23);
+    const uint32_t imask = hdr >> 24;
+    const float ax = sx * r.inv.x, ay = sy * r.inv.y, az = sz * r.inv.z;
+    const float bx = (w0.x - r.o.x) * r.inv.x, by = (w0.y - r.o.y) * r.inv.y, bz = (w0.z - r.o.z) * r.inv.z;
+    // near planes are the lower ones along a positive direction component
+    const uint32_t wx[4] = {__float_as_uint(w1.x), __float_as_uint(w1.y), __float_as_uint(w1.z), __float_as_uint(w1.w)};
+    const uint32_t wy[4] = {__float_as_uint(w2.x), __float_as_uint(w2.y), __float_as_uint(w2.z), __float_as_uint(w2.w)};
+    const uint32_t wz[4] = {__float_as_uint(w3.x), __float_as_uint(w3.y), __float_as_uint(w3.z), __float_as_uint(w3.w)};
+    const uint32_t nx0 = nx ? wx[2] : wx[0], nx1 = nx ? wx[3] : wx[1], fx0 = nx ? wx[0] : wx[2], fx1 = nx ? wx[1] : wx[3];
+    const uint32_t ny0 = ny ? wy[2] : wy[0], ny1 = ny ? wy[3] : wy[1], fy0 = ny ? wy[0] : wy[2], fy1 = ny ? wy[1] : wy[3];
+    const uint32_t nz0 = nz ? wz[2] : wz[0], nz1 = nz ? wz[3] : wz[1], fz0 = nz ? wz[0] : wz[2], fz1 = nz ? wz[1] : wz[3];
+    float tn[8];
+    uint32_t hit = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const uint32_t nxw = k < 4 ? nx0 : nx1, fxw = k < 4 ? fx0 : fx1;
+        const uint32_t nyw = k < 4 ? ny0 : ny1, fyw = k < 4 ? fy0 : fy1;
+        const uint32_t nzw = k < 4 ? nz0 : nz1, fzw = k < 4 ? fz0 : fz1;
+        const int b = k & 3;
+        const float tnx = fmaf(byte_f(nxw, b), ax, bx), tfx = fmaf(byte_f(fxw, b), ax, bx);
+        const float tny = fmaf(byte_f(nyw, b), ay, by), tfy = fmaf(byte_f(fyw, b), ay, by);
+        const float tnz = fmaf(byte_f(nzw, b), az, bz), tfz = fmaf(byte_f(fzw, b), az, bz);
+        const float tnear = fmax3(tnx, tny, fmaxf(tnz, 0.0f));
+        const float tfar = fmin3(tfx, tfy, fminf(tfz, q.best_t));
+        tn[k] = tnear;
+        hit |= (tnear <= tfar * k_box_pad ? 1u : 0u) << k;
+    }
+    const int refs[8] = {w4.x, w4.y, w4.z, w4.w, w5.x, w5.y, w5.z, w5.w};
+    // leaves first: a hit found here shortens every interval tested after it
+    uint32_t lm = mask_xor_permute(hit & ~imask, q.oct);
+    while (lm) {
+        const uint32_t p = 31u - __clz(lm);
+        lm &= ~(1u << p);
+        if (wide_leaf<ANY, STATS>(tris, r, sel8(refs, p ^ q.oct), q.tmax, q.exclude, q.best_t, q.best, q.bu, q.bv,
+                                  cnt)) {
+            q.node = -1;
+            return true;
+        }
+    }
+    // internal children: push all but the first-ranked, lowest rank first
+    uint32_t im = mask_xor_permute(hit & imask, q.oct);
+    int next = -1;
+    while (im) {
+        const uint32_t p = __ffs(im) - 1;
+        im &= im - 1u;
+        const uint32_t s = p ^ q.oct;
+        const float t = sel8(tn, s);
+        if (t >= q.best_t) continue;
+        const int ref = sel8(refs, s);
+        if (im) {
+            if (q.sp >= k_wide_stack) {
+                err |= k_deverr_stack;
+                q.node = -1;
+                return true;
+            }
+            stack[q.sp++] = make_int2(ref, __float_as_int(t));
+        } else {
+            next = ref;
+        }
+    }
+    if (next < 0) {
+        while (q.sp > 0) {
+            const int2 e = stack[--q.sp];
+            if (__int_as_float(e.y) < q.best_t) {
+                next = e.x;
+                break;
+            }
+        }
+    }
+    q.node = next;
+    return next < 0;
+}
+
+// Whole-ray traversal of the 8-wide BVH; same contract as trace_bvh (trace.cuh):
+// ANY = true stops at the first hit with t in (0, tmax). Returns the original index of the
+// hit triangle (or -1), its distance in t_out and its barycentrics in bu, bv.
+template <bool ANY, bool STATS>
+__device__ __forceinline__ int trace_wide(const float4* __restrict__ wide, const float4* __restrict__ tris,
+                                          uint32_t n_tris, const RayInv& r, float tmax, int exclude, float& t_out,
+                                          float& bu, float& bv, uint32_t& err, TraceCounters& cnt) {
+    WideRay q;
+    wide_begin(q, r.o, r.d, tmax, exclude, n_tris);
+    int2 stack[k_wide_stack];
+    while (!wide_visit<ANY, STATS>(wide, tris, q, stack, err, cnt)) {
+    }
+    t_out = q.best_t;
+    bu = q.bu;
+    bv = q.bv;
+    return q.best;
+}
+
+// Warp-batch persistent traversal of a ray queue over the 8-wide records: a warp takes 32
+// consecutive rays with one atomic and traces each to completion (Job as in trace_batches).
+template <bool ANY, bool STATS, class Job>
+__device__ __forceinline__ void trace_batches_wide(Job& job, const float4* __restrict__ wide,
+                                                   const float4* __restrict__ tris, uint32_t n_tris, int n,
+                                                   int* __restrict__ fetch, uint32_t& err, TraceCounters& cnt) {
+    const int lane = threadIdx.x & 31;
+    while (true) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(fetch, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const int i = base + lane;
+        if (i < n) {
+            float3 o, d;
+            float tmax;
+            int exclude;
+            job.load(i, o, d, tmax, exclude);
+            TraceState s;
+            s.r = make_ray(o, d);
+            s.tmax = tmax;
+            s.best = trace_wide<ANY, STATS>(wide, tris, n_tris, s.r, tmax, exclude, s.best_t, s.bu, s.bv, err, cnt);
+            job.store(i, s);
+        }
+    }
+}
+
+// Persistent traversal of a ray queue with per-lane refill: once `refill` lanes of a warp
+// are idle they take the next rays with one atomic, while the other lanes carry on with
+// their own rays (refill = 32 waits for the whole warp). Job as in trace_batches. Every
+// lane of the warp must call this (it uses full-warp votes).
+template <bool ANY, bool STATS, class Job>
+__device__ __forceinline__ void trace_wide_refill(Job& job, const float4* __restrict__ wide,
+                                                  const float4* __restrict__ tris, uint32_t n_tris, int n, int refill,
+                                                  int* __restrict__ fetch, uint32_t& err, TraceCounters& cnt) {
+    const int lane = threadIdx.x & 31;
+    WideRay q;
+    int2 stack[k_wide_stack];
+    bool active = false, exhausted = false;
+    int idx = 0;
+    while (true) {
+        const uint32_t idle = __ballot_sync(0xffffffffu, !active);
+        if (!exhausted && __popc(idle) >= refill) {
+            const int leader = __ffs(idle) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(fetch, __popc(idle));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            exhausted = base + __popc(idle) >= n;
+            if (!active) {
+                idx = base + __popc(idle & lanemask_lt());
+                if (idx < n) {
+                    float3 o, d;
+                    float tmax;
+                    int exclude;
+                    job.load(idx, o, d, tmax, exclude);
+                    wide_begin(q, o, d, tmax, exclude, n_tris);
+                    active = true;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) break;
+        if (active && wide_visit<ANY, STATS>(wide, tris, q, stack, err, cnt)) {
+            TraceState s;
+            s.r = q.r;
+            s.tmax = q.tmax;
+            s.best_t = q.best_t;
+            s.best = q.best;
+            s.bu = q.bu;
+            s.bv = q.bv;
+            job.store(idx, s);
+            active = false;
+        }
+    }
+}
+
+}  // namespace quasi

@@ -303,6 +303,12 @@ class PluginHost:
                                                                 bounds.ctypes.data))
         return {"morton": morton, "order": order, "children": children, "boxes": boxes, "bounds": bounds}
 
+    def read_wide_bvh(self, n: int) -> np.ndarray:
+        """The 8-wide traversal records, (max(n - 1, 1), 24) uint32."""
+        words = np.zeros((max(n - 1, 1), 24), np.uint32)
+        self._check("Q_cuda_read_wide_bvh", self.lib.Q_cuda_read_wide_bvh(self.handle, words.ctypes.data))
+        return words
+
     def read_samples(self, spp: int) -> tuple[np.ndarray, np.ndarray]:
         n = self.width * self.height * spp
         rad = np.zeros(3 * n, np.float32)

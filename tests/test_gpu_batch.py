@@ -89,6 +89,10 @@ def test_batch_waves_split_samples_and_scenes(scenes, single):
     dict(use_graph=2, form=1),
     dict(trace_block=256, fetch_rays=128, wave_paths=50000),
     dict(collect_stats=1),
+    dict(refill_lanes=1),
+    dict(refill_lanes=32, trace_block=64),
+    dict(bvh_width=2),
+    dict(bvh_width=2, fetch_rays=64, collect_stats=1),
 ])
 def test_batch_forms_and_launch_modes(scenes, single, opts):
     host = q.PluginHost()
@@ -104,9 +108,10 @@ def test_batch_autotune_keeps_images(scenes, single):
         chosen = b.autotune(budget_ms=3000)
         assert chosen.form in (0, 1)
         assert chosen.trace_block in (64, 128, 256) and chosen.fetch_rays in (32, 64, 128)
+        assert chosen.bvh_width == 8 and chosen.refill_lanes in (4, 8, 16)
         o = b.options()
-        assert (o.form, o.trace_block, o.fetch_rays, o.wave_paths) == (chosen.form, chosen.trace_block,
-                                                                       chosen.fetch_rays, chosen.wave_paths)
+        assert (o.form, o.trace_block, o.fetch_rays, o.wave_paths, o.refill_lanes) == (
+            chosen.form, chosen.trace_block, chosen.fetch_rays, chosen.wave_paths, chosen.refill_lanes)
         b.render()
         b.synchronize()
         for i, (ref1, _, _, _) in enumerate(single):
@@ -146,9 +151,11 @@ def test_batch_backward_matches_single_scene_adjoint(scenes):
             rc = single.lib.Q_cuda_backward(single.handle, gs.data_ptr(), spp, 0, ra.data_ptr(), re.data_ptr(), stream)
             assert rc == 0
             torch.cuda.synchronize()
-            # float atomics add in a different order: equal to rounding
-            torch.testing.assert_close(ga[t0:t0 + n], ra, rtol=1e-4, atol=1e-6)
-            torch.testing.assert_close(ge[t0:t0 + n], re, rtol=1e-4, atol=1e-6)
+            # float atomics add in a different order: equal to rounding of sums whose terms
+            # cancel (random-signed image gradient), so the absolute tolerance scales with the
+            # largest gradient entry of the scene
+            torch.testing.assert_close(ga[t0:t0 + n], ra, rtol=1e-4, atol=1e-4 * float(ra.abs().max()) + 1e-9)
+            torch.testing.assert_close(ge[t0:t0 + n], re, rtol=1e-4, atol=1e-4 * float(re.abs().max()) + 1e-9)
             single.destroy()
     host.destroy()
 
@@ -162,6 +169,10 @@ def test_batch_rejects_bad_input(scenes):
         q.Batch(host, [(sc, 64, 64, 1)], trace_block=48)
     with pytest.raises(q.QuasiError):
         q.Batch(host, [(sc, 64, 64, 1)], fetch_rays=40)
+    with pytest.raises(q.QuasiError):
+        q.Batch(host, [(sc, 64, 64, 1)], bvh_width=4)
+    with pytest.raises(q.QuasiError):
+        q.Batch(host, [(sc, 64, 64, 1)], refill_lanes=33)
     with q.Batch(host, [(sc, 64, 64, 1)], max_depth=4) as b:
         with pytest.raises(q.QuasiError) as e:
             b.backward(1, None, None)  # nothing rendered since the reset

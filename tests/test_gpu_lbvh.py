@@ -1,4 +1,5 @@
-"""GPU LBVH and radix sort, bit-exact against the oracle and numpy (integer work)."""
+"""GPU LBVH and radix sort, bit-exact against the oracle and numpy (integer work), and the
+8-wide traversal records collapsed from the LBVH, bit-exact against the oracle's collapse."""
 from __future__ import annotations
 
 import ctypes as C
@@ -33,6 +34,11 @@ def _compare(host, orc, scene: q.Scene) -> None:
     assert np.array_equal(g["order"], o["order"]), "sort order differs"
     assert np.array_equal(g["children"], o["children"]), "topology differs"
     assert np.array_equal(g["boxes"].view(np.uint32), o["boxes"].view(np.uint32)), "child boxes differ"
+    gw = host.read_wide_bvh(scene.tri_count)
+    ow = orc.collapse8(scene.vertices)
+    reach = orc.wide_reachable(ow)
+    assert orc.wide_reachable(gw) == reach
+    assert np.array_equal(gw[reach], ow[reach]), "8-wide records differ"
     assert host.stats().error_flags == 0
 
 

@@ -248,3 +248,25 @@ def test_autotune_keeps_images(cuda_ok):
     assert np.array_equal(h.readback(), ref)
     assert h.stats().error_flags == 0
     h.destroy()
+
+
+@pytest.mark.parametrize("spec,w,h,spp,depth", [("cornell36", 128, 128, 8, 4), ("soup:n=200000,seed=5", 320, 180, 4, 8)])
+def test_wide_and_binary_traversal_agree(host, spec, w, h, spp, depth):
+    """The 8-wide records and the binary LBVH return the same closest hits (smallest t, ties
+    to the lower triangle index) and the same shadow-ray outcomes: both forms give the same
+    path signatures and the same radiance bits, in the wavefront and the megakernel."""
+    scene = q.make_scene(spec, host.lib)
+    out = {}
+    for width, mega in ((2, 0), (8, 0), (8, 1)):
+        img, rad, sig, st = _render(host, scene, w, h, spp, depth, seed=11, bvh_width=width, megakernel=mega)
+        out[(width, mega)] = (img, rad, sig, st)
+    img2, rad2, sig2, st2 = out[(2, 0)]
+    for key in ((8, 0), (8, 1)):
+        img8, rad8, sig8, st8 = out[key]
+        same = sig8 == sig2
+        assert same.mean() >= 1.0 - 1e-5, (key, same.mean())
+        assert np.array_equal(rad8[same], rad2[same]), key
+        assert st8.camera_rays == st2.camera_rays
+        if same.all():
+            assert np.array_equal(img8, img2), key
+    host.set_options(bvh_width=0, megakernel=0)
