@@ -168,7 +168,7 @@ __device__ __forceinline__ void trace_wide_refill_multi(Job& job, const BatchSce
 // WIDE: per-lane refill over the 8-wide records (refill = idle lanes that trigger a fetch);
 // otherwise warp chunks over the scenes' binary LBVHs.
 template <bool STATS, bool WIDE>
-__global__ void __launch_bounds__(256) k_batch_trace_closest(const BatchSceneDev* __restrict__ scenes,
+__global__ void __launch_bounds__(256, WIDE ? QUASI_WIDE_MIN_BLOCKS : 1) k_batch_trace_closest(const BatchSceneDev* __restrict__ scenes,
                                                              const uint2* __restrict__ meta, const float4* __restrict__ q,
                                                              float4* __restrict__ hits, const int* __restrict__ count,
                                                              int capacity, int chunk, int refill, int* __restrict__ fetch,
@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(256) k_batch_trace_closest(const BatchSceneDev
 }
 
 template <bool STATS, bool WIDE>
-__global__ void __launch_bounds__(256) k_batch_trace_shadow(const BatchSceneDev* __restrict__ scenes,
+__global__ void __launch_bounds__(256, WIDE ? QUASI_WIDE_MIN_BLOCKS : 1) k_batch_trace_shadow(const BatchSceneDev* __restrict__ scenes,
                                                             const uint2* __restrict__ meta, PathDev p,
                                                             const float4* __restrict__ sq, const int* __restrict__ count,
                                                             int capacity, int chunk, int refill,

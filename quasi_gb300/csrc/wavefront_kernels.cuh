@@ -47,13 +47,6 @@ __global__ void __launch_bounds__(256) k_camera(FrameParams f, PathDev p, float4
     }
 }
 
-// Minimum resident 256-thread blocks per SM asked of the compiler for the 8-wide trace
-// kernels, a register cap (4 -> 64 registers per thread). Uncapped, they take 93 registers
-// and 5 blocks of 128 threads fit an SM; at 64 registers (a few bytes of spills) 8 fit, and
-// the 1M-triangle frame renders 18% faster on GB300.
-#ifndef QUASI_WIDE_MIN_BLOCKS
-#define QUASI_WIDE_MIN_BLOCKS 4
-#endif
 constexpr int trace_min_blocks(int mode) { return mode >= k_mode_wide ? QUASI_WIDE_MIN_BLOCKS : 1; }
 
 // Persistent closest-hit traversal.
@@ -118,7 +111,14 @@ __global__ void k_tally(const int* __restrict__ counters, uint32_t waves, uint32
     if (threadIdx.x == 0) stats[4] += sum;
 }
 
-__global__ void __launch_bounds__(256) k_shade(FrameParams f, SceneDev s, PathDev p, uint32_t bounce,
+// Minimum resident 256-thread blocks per SM asked of the compiler for k_shade (a register
+// cap). With 1 it takes 141 registers and the 1080p frame's shading costs 138 ms; 2 blocks
+// (128 registers) or 4 (64, with spills) cost 101 ms on GB300.
+#ifndef QUASI_SHADE_MIN_BLOCKS
+#define QUASI_SHADE_MIN_BLOCKS 2
+#endif
+
+__global__ void __launch_bounds__(256, QUASI_SHADE_MIN_BLOCKS) k_shade(FrameParams f, SceneDev s, PathDev p, uint32_t bounce,
                                                const float4* __restrict__ q, const float4* __restrict__ hits,
                                                const int* __restrict__ count, int capacity, float4* __restrict__ next_q,
                                                int* __restrict__ next_count, float4* __restrict__ shadow_q,
