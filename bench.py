@@ -92,6 +92,21 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def replica_totals(total_ms: float, rays: int, device) -> tuple[float, int]:
+    """Replicas: every rank renders its own frames (own seeds), nothing is exchanged on the
+    data path. The job's time is the slowest rank's and its rays are every rank's."""
+    import torch
+    import torch.distributed as dist
+
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return total_ms, rays
+    t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+    r = torch.tensor([float(rays)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(r)
+    return float(t.item()), int(r.item())
+
+
 def _dist():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -405,14 +420,7 @@ def run_ours(args) -> None:
     times = host.kernel_times(reset=True)
     opts["profile"] = 0
     host.set_options(seed=0, **opts)
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([total_ms], device="cuda")
-        r = torch.tensor([float(rays)], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dist.all_reduce(r)
-        total_ms, rays = float(t.item()), int(r.item())
+    total_ms, rays = replica_totals(total_ms, rays, "cuda")
     value = rays / (total_ms / 1e3) / 1e6
 
     # end to end through the plugin ABI: pinned host scene upload + render + host readback

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdint>
 #include <cstdio>
@@ -11,6 +12,17 @@
 #include <vector>
 
 namespace quasi {
+
+// NVTX range over a host scope (frame, LBVH build, wave): lets a profiler attribute and
+// filter the launches inside it (ncu --nvtx --nvtx-include "quasi.wave/"). Without an
+// attached tool the calls return at once.
+class NvtxRange {
+public:
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 class KernelProfiler {
 public:

@@ -275,6 +275,7 @@ uint32_t Renderer::effective_wave_spp(uint32_t spp) const {
 }
 
 int Renderer::render(const Q_render_frame& fr) {
+    NvtxRange frame_range("quasi.frame");
     error_.clear();
     if (!has_scene_) return fail(QUASI_ERR_STATE, "no scene");
     if (fr.width == 0 || fr.height == 0) return fail(QUASI_ERR_INVALID, "zero-sized frame");
@@ -292,6 +293,7 @@ int Renderer::render(const Q_render_frame& fr) {
     R_TRY(cudaEventRecord(ev_frame0_, s), "event");
     bvh_timed_ = false;
     if (opt_.integrator == QUASI_INTEGRATOR_NEE && (bvh_dirty_ || opt_.rebuild_each_frame)) {
+        NvtxRange bvh_range("quasi.lbvh");
         R_TRY(cudaEventRecord(ev_bvh0_, s), "event");
         R_TRY(bvh_.build(tri_in_.as<float4>(), n_tris_, s, prof_, err_dev_.as<uint32_t>()), "lbvh build");
         const int levels = opt_.smem_levels ? static_cast<int>(opt_.smem_levels) : k_default_smem_levels;
@@ -405,6 +407,7 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
     const int cap = static_cast<int>(slots * S);
 
     for (uint32_t w = 0; w < waves; ++w) {
+        NvtxRange wave_range("quasi.wave");
         const uint32_t Sw = std::min(S, spp - w * S);
         f.wave_spp = Sw;
         f.sample_base = samples_ + w * S;

@@ -192,6 +192,7 @@ __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, cons
         hit |= (tnear <= tfar * k_box_pad ? 1u : 0u) << k;
     }
     const int refs[8] = {w4.x, w4.y, w4.z, w4.w, w5.x, w5.y, w5.z, w5.w};
+    uint32_t im = mask_xor_permute(hit & imask, q.oct);
     // leaves first: a hit found here shortens every interval tested after it
     uint32_t lm = mask_xor_permute(hit & ~imask, q.oct);
     while (lm) {
@@ -204,7 +205,6 @@ __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, cons
         }
     }
     // internal children: push all but the first-ranked, lowest rank first
-    uint32_t im = mask_xor_permute(hit & imask, q.oct);
     int next = -1;
     while (im) {
         const uint32_t p = __ffs(im) - 1;
