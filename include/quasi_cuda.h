@@ -358,7 +358,7 @@ typedef struct Q_cuda_batch_options {
     uint32_t max_depth;     /* path vertices after the camera (6) */
     uint32_t seed;          /* RNG seed, shared by all scenes (0) */
     uint32_t form;          /* QUASI_BATCH_WAVEFRONT (default) or QUASI_BATCH_MEGAKERNEL */
-    uint32_t wave_paths;    /* path slots per wave (0 = 32M; raised to the largest sample plane) */
+    uint32_t wave_paths;    /* path slots per wave (0 = 64M; raised to the largest sample plane) */
     uint32_t trace_block;   /* threads per block of the persistent kernels (0 = 128) */
     uint32_t fetch_rays;    /* rays or paths a warp takes per atomic, multiple of 32 (0 = 32) */
     uint32_t use_graph;     /* 0 = default (graph), 1 = graph, 2 = plain launches */

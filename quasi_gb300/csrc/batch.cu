@@ -21,7 +21,7 @@ CameraFF make_camera_basis(const Q_camera& c, uint32_t w, uint32_t h);  // wavef
 namespace {
 
 inline uint32_t ceil_div(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
-constexpr uint32_t k_default_wave_paths = 32u << 20;  // as the single-scene renderer's waves
+constexpr uint32_t k_default_wave_paths = 64u << 20;  // as the single-scene renderer's waves
 constexpr uint32_t k_max_wave_paths = 1u << 26;
 
 }  // namespace
@@ -205,7 +205,8 @@ int BatchRenderer::upload_table() {
                        k_trace_steps,
                        nullptr,
                        0,
-                       opt_.bvh_width == 2 ? nullptr : bv.wide};
+                       opt_.bvh_width == 2 ? nullptr : bv.wide,
+                       bv.tri_nrm};
         d.px_offset = h.px_offset;
         d.tri_offset = h.tri_offset;
         d.spp = h.spp;
@@ -674,7 +675,7 @@ int BatchRenderer::autotune(double budget_ms, Q_cuda_batch_options* chosen) {
     int rc = measure(best, best_ms);
     if (rc) return rc;
     const uint32_t forms[] = {QUASI_BATCH_WAVEFRONT, QUASI_BATCH_MEGAKERNEL};
-    const uint32_t waves[] = {4u << 20, 8u << 20, 16u << 20, 32u << 20};
+    const uint32_t waves[] = {8u << 20, 16u << 20, 32u << 20, 64u << 20};
     const uint32_t blocks[] = {64, 128, 256};
     const uint32_t fetches[] = {32, 64, 128};
     const uint32_t refills[] = {4, 8, 16};

@@ -4,6 +4,7 @@
 // Morton codes, the sort order and the topology bit-exact against the oracle.
 #include "bvh.cuh"
 #include "common.cuh"
+#include "ffmath.cuh"
 #include "wide.cuh"
 
 #include <algorithm>
@@ -473,6 +474,22 @@ __global__ void __launch_bounds__(128) k_collapse8(const float4* __restrict__ no
     w[5] = make_float4(__int_as_float(refs[4]), __int_as_float(refs[5]), __int_as_float(refs[6]), __int_as_float(refs[7]));
 }
 
+// Shading geometry of triangle i (original order): ng = cross(e1, e2) in double-float from
+// the exact edge differences, its length |ng| and the unit normal ng / |ng| (one reciprocal).
+__global__ void __launch_bounds__(256) k_tri_normals(const float4* __restrict__ tri_in, uint32_t n,
+                                                     float4* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float3 a = xyz(__ldg(&tri_in[3 * i]));
+    const ff3 e1 = ff3_diff(xyz(__ldg(&tri_in[3 * i + 1])), a);
+    const ff3 e2 = ff3_diff(xyz(__ldg(&tri_in[3 * i + 2])), a);
+    const ff3 ng = ff3_cross(e1, e2);
+    const ff len = ff3_length(ng);
+    const ff3 u = ff3_scale(ng, ff_div(ffv(1.0f), len));
+    out[2 * i] = make_float4(u.x.hi, u.x.lo, u.y.hi, u.y.lo);
+    out[2 * i + 1] = make_float4(u.z.hi, u.z.lo, len.hi, len.lo);
+}
+
 // Copies the first `count` internal nodes in breadth-first order (the top levels of the
 // tree) into `tree`, rewriting child links that stay inside the copy to k_tree_flag | slot.
 // One thread: count is at most a few hundred. The queue of global indices lives in the
@@ -586,6 +603,7 @@ cudaError_t LbvhBuilder::reserve(uint32_t n) {
     QUASI_TRY_CUDA(cudaMalloc(&nodes_, sizeof(float4) * 4 * m));
     QUASI_TRY_CUDA(cudaMalloc(&tris_, sizeof(float4) * 3 * m));
     QUASI_TRY_CUDA(cudaMalloc(&wide_, sizeof(float4) * k_wide_node_f4 * m));
+    QUASI_TRY_CUDA(cudaMalloc(&tri_nrm_, sizeof(float4) * 2 * m));
     QUASI_TRY_CUDA(radix_sort_reserve(sort_, m));
     capacity_ = m;
     return cudaSuccess;
@@ -595,12 +613,12 @@ void LbvhBuilder::release() {
     for (void* p : {static_cast<void*>(bounds_), static_cast<void*>(partial_), static_cast<void*>(morton_),
                     static_cast<void*>(keys_), static_cast<void*>(order_), static_cast<void*>(parent_),
                     static_cast<void*>(flags_), static_cast<void*>(nodes_), static_cast<void*>(tris_),
-                    static_cast<void*>(wide_)})
+                    static_cast<void*>(wide_), static_cast<void*>(tri_nrm_)})
         if (p) cudaFree(p);
     bounds_ = partial_ = nullptr;
     morton_ = keys_ = order_ = flags_ = nullptr;
     parent_ = nullptr;
-    nodes_ = tris_ = wide_ = nullptr;
+    nodes_ = tris_ = wide_ = tri_nrm_ = nullptr;
     if (tree_) cudaFree(tree_);
     tree_ = nullptr;
     tree_n_ = tree_capacity_ = 0;
@@ -614,6 +632,8 @@ cudaError_t LbvhBuilder::build(const float4* tri_in, uint32_t n, cudaStream_t st
     QUASI_TRY_CUDA(reserve(n));
     n_ = n;
     if (n == 0) return cudaSuccess;
+    QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "tri_normals", stream,
+                                (k_tri_normals<<<ceil_div(n, 256), 256, 0, stream>>>(tri_in, n, tri_nrm_))));
     const int parts = static_cast<int>(std::min<uint32_t>(k_bounds_blocks, ceil_div(n, 256)));
     QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_bounds", stream,
                                 (k_bounds_partial<<<parts, 256, 0, stream>>>(tri_in, n, partial_))));

@@ -9,6 +9,8 @@
 //   5. bottom-up child boxes with per-node arrival counters; triangles gathered into
 //      leaf order as {v0, orig index}, {e1}, {e2}
 //   6. the 8-wide traversal records collapsed from the binary nodes (wide.cuh)
+//   7. per-triangle shading geometry: the unit normal of cross(e1, e2) and its length in
+//      double-float, read by every shading step instead of recomputing them
 //
 // Node layout, 64 bytes (4 x float4), child boxes stored in the parent:
 //   n0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
@@ -50,6 +52,8 @@ struct LbvhView {
     const float4* tree = nullptr;   // top levels in breadth-first order (for shared memory)
     int tree_n = 0;                 // nodes in `tree`
     const float4* wide = nullptr;   // 8-wide records (wide.cuh), one per internal node
+    const float4* tri_nrm = nullptr; // per triangle (original order), 2 float4: the unit normal
+                                     // of cross(e1, e2) and that vector's length, double-float
 };
 
 class LbvhBuilder {
@@ -70,7 +74,7 @@ public:
     cudaError_t build_treelet(int max_nodes, cudaStream_t stream, KernelProfiler& prof);
 
     LbvhView view() const {
-        return LbvhView{nodes_, tris_, n_, n_ == 0 ? 0u : (n_ > 1 ? n_ - 1 : 1u), tree_, tree_n_, wide_};
+        return LbvhView{nodes_, tris_, n_, n_ == 0 ? 0u : (n_ > 1 ? n_ - 1 : 1u), tree_, tree_n_, wide_, tri_nrm_};
     }
 
     // Debug copies to host (stream-synchronous).
@@ -92,6 +96,7 @@ private:
     float4* nodes_ = nullptr;
     float4* tris_ = nullptr;
     float4* wide_ = nullptr;         // 8-wide records, 96 bytes per internal node
+    float4* tri_nrm_ = nullptr;      // 32 bytes per triangle (shading normals and areas)
     float4* tree_ = nullptr;
     int tree_n_ = 0;
     int tree_capacity_ = 0;

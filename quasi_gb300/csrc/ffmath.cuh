@@ -156,9 +156,10 @@ __device__ __forceinline__ ff3 ff3_cross(const ff3& a, const ff3& b) {
                ff_sub(ff_mul(a.x, b.y), ff_mul(a.y, b.x))};
 }
 __device__ __forceinline__ ff ff3_length(const ff3& a) { return ff_sqrt(ff3_dot(a, a)); }
+// One double-float division (the reciprocal of the length) and three products: a third of
+// the cost of three divisions, and the same ~1e-14 relative accuracy.
 __device__ __forceinline__ ff3 ff3_normalize(const ff3& a) {
-    const ff len = ff3_length(a);
-    return ff3{ff_div(a.x, len), ff_div(a.y, len), ff_div(a.z, len)};
+    return ff3_scale(a, ff_div(ffv(1.0f), ff3_length(a)));
 }
 
 // Packed storage of a double-float ray (origin, direction) in 3 float4.

@@ -47,6 +47,7 @@ struct SceneDev {
     int tree_n;             // nodes in `tree` (0 = no staging)
     const float4* wide;     // 8-wide traversal records (wide.cuh) for the wavefront trace
                             // kernels, or null: they traverse `nodes`
+    const float4* tri_nrm;  // per triangle: unit normal and |cross(e1, e2)|, double-float
 };
 
 // Copies the treelet into the block's shared memory (dynamic size tree_n * 64 bytes).
@@ -214,7 +215,7 @@ struct HitShade {
 // Updates beta, the signature and the stored double-float ray of the path.
 __device__ __forceinline__ void shade_hit(const FrameParams& f, const SceneDev& s, const PathDev& p, uint32_t bounce,
                                           int pid, uint32_t local, float4 h, HitShade& o) {
-    const VertexScene vs{s.tri_in, s.albedo, s.emission, s.emitters, s.n_emit, f.eps};
+    const VertexScene vs{s.tri_in, s.tri_nrm, s.albedo, s.emission, s.emitters, s.n_emit, f.eps};
     const int prim = __float_as_int(h.y);
     ff3 ro, rd;
     ff_ray_load(&p.ray_ff[3ull * pid], ro, rd);
@@ -322,7 +323,7 @@ __device__ __forceinline__ float3 trace_path(const FrameParams& f, const SceneDe
                                              uint32_t sample, PathVertex* verts, int& n_verts, float4* aov_a,
                                              float4* aov_n, uint32_t* sig_out, uint32_t& err, TraceCounters& cnt,
                                              int& rays, int& shadow_rays) {
-    const VertexScene vs{s.tri_in, s.albedo, s.emission, s.emitters, s.n_emit, f.eps};
+    const VertexScene vs{s.tri_in, s.tri_nrm, s.albedo, s.emission, s.emitters, s.n_emit, f.eps};
     ff3 ro, rd;
     camera_ray_ff(f, x, y, sample, ro, rd);
     float3 beta = mk3(1.f, 1.f, 1.f), L = mk3(0.f, 0.f, 0.f);

@@ -4,7 +4,8 @@
 //
 // Per vertex k of a path (hit triangle h, incoming double-float ray ro + t rd):
 //   x   = plane(h) intersected with the double-float ray        (hit point)
-//   n   = normalize(cross(e1, e2)) flipped to face the ray       (plugin.mm:192)
+//   n   = normalize(cross(e1, e2)) flipped to face the ray       (plugin.mm:192); the unit
+//         normals and |cross(e1, e2)| come from a per-triangle table built with the LBVH
 //   key = path_key(seed, pixel, sample, k);  sel = pcg(key); r1, r2, r3, r4 chained
 //   NEE: light l = emitters[(sel * n_emit) >> 32], point y = v0 + su(1-r2) e1 + su r2 e2,
 //        su = sqrt(r1); g = cos_x cos_l / d^2 * area * n_emit / pi, skipped when l == h or a
@@ -23,6 +24,7 @@ namespace quasi {
 
 struct VertexScene {
     const float4* tri_in;   // original order, v0 v1 v2
+    const float4* tri_nrm;  // original order: unit normal of cross(e1, e2), |cross(e1, e2)|
     const float4* albedo;
     const float4* emission;
     const int* emitters;
@@ -41,23 +43,29 @@ struct VertexResult {
     ff3 dir;           // continuation direction (valid when want_dir)
 };
 
+// Unit normal and |cross(e1, e2)| (twice the area) of triangle i from the shading table.
+__device__ __forceinline__ ff3 tri_unit_normal(const float4* __restrict__ tri_nrm, int i, ff& area2) {
+    const float4 p = __ldg(&tri_nrm[2 * i]), q = __ldg(&tri_nrm[2 * i + 1]);
+    area2 = ff{q.z, q.w};
+    return ff3{ff{p.x, p.y}, ff{p.z, p.w}, ff{q.x, q.y}};
+}
+
 // hit: (t, prim, u, v) from the FP32 traversal; ro, rd: the double-float ray that found it.
 __device__ __forceinline__ void shade_vertex(const VertexScene& s, uint32_t key, int prim, float4 hit, const ff3& ro,
                                              const ff3& rd, bool want_dir, VertexResult& out) {
     const float3 a = xyz(__ldg(&s.tri_in[3 * prim]));
-    const ff3 e1 = ff3_diff(xyz(__ldg(&s.tri_in[3 * prim + 1])), a);
-    const ff3 e2 = ff3_diff(xyz(__ldg(&s.tri_in[3 * prim + 2])), a);
-    const ff3 ng = ff3_cross(e1, e2);
+    ff area_h;
+    ff3 nrm = tri_unit_normal(s.tri_nrm, prim, area_h);
     // Re-intersect the hit triangle's plane with the double-float ray.
-    const ff den = ff3_dot(ng, rd);
+    const ff den = ff3_dot(nrm, rd);
     ff3 x;
     if (den.hi != 0.0f) {
-        const ff t = ff_div(ff3_dot(ng, ff3_sub(ff3v(a), ro)), den);
+        const ff t = ff_div(ff3_dot(nrm, ff3_sub(ff3v(a), ro)), den);
         x = ff3_add(ro, ff3_scale(rd, t));
     } else {
-        x = ff3v(a + ff3_f(e1) * hit.z + ff3_f(e2) * hit.w);
+        const float3 e1 = xyz(__ldg(&s.tri_in[3 * prim + 1])) - a, e2 = xyz(__ldg(&s.tri_in[3 * prim + 2])) - a;
+        x = ff3v(a + e1 * hit.z + e2 * hit.w);
     }
-    ff3 nrm = ff3_normalize(ng);
     if (den.hi > 0.0f) nrm = ff3_neg(nrm);
     out.nrm = ff3_f(nrm);
     uint32_t st = key;
@@ -85,17 +93,17 @@ __device__ __forceinline__ void shade_vertex(const VertexScene& s, uint32_t key,
             const ff dist = ff_sqrt(d2);
             const ff3 wi = ff3_scale(dv, ff_div(ffv(1.0f), dist));
             const ff cos_x = ff3_dot(nrm, wi);
-            const ff3 nl = ff3_cross(le1, le2);
-            const ff area2 = ff3_length(nl);
+            ff area2;
+            const ff3 nl = tri_unit_normal(s.tri_nrm, l, area2);
             const ff cl = ff3_dot(nl, wi);
-            const float cos_l = fabsf(ff_f(ff_div(cl, area2)));
+            const float cos_l = fabsf(ff_f(cl));
             if (cos_x.hi > 0.0f && cos_l > 0.0f && d2.hi > 0.0f) {
                 out.g = ff_f(cos_x) * cos_l / ff_f(d2) * (0.5f * ff_f(area2)) * static_cast<float>(s.n_emit) * k_inv_pi;
                 // The shadow ray runs from the light sample, lifted by eps along the light's
                 // normal towards the shading side, to just short of the lifted shading point:
                 // neither end's plane (nor a coplanar neighbour) can be crossed.
                 const float side = cl.hi < 0.0f ? s.eps : -s.eps;
-                const ff3 so = ff3_add(yl, ff3_scale(nl, ff_div(ffv(side), area2)));
+                const ff3 so = ff3_add(yl, ff3_scale(nl, side));
                 const ff3 sd = ff3_sub(out.org, so);
                 const ff sdist = ff3_length(sd);
                 out.so = ff3_f(so);

@@ -359,7 +359,8 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
                 opt_.trace_steps ? static_cast<int>(opt_.trace_steps) : k_trace_steps,
                 wide ? nullptr : bv.tree,
                 wide ? 0 : bv.tree_n,
-                wide ? bv.wide : nullptr};
+                wide ? bv.wide : nullptr,
+                bv.tri_nrm};
     const size_t tree_smem = sizeof(float4) * 4 * static_cast<size_t>(sd.tree_n);
     PathDev pd{beta_.as<float4>(),  lpath_.as<float4>(), aov_a_.as<float4>(),
                aov_n_.as<float4>(), ray_ff_.as<float4>(), opt_.record_samples ? sig_.as<uint32_t>() : nullptr};
@@ -459,7 +460,7 @@ SceneDev Renderer_scene_dev(const LbvhView& bv, const DeviceBuffer& tri_in, cons
                             uint32_t bvh_width) {
     return SceneDev{tri_in.as<float4>(), albedo.as<float4>(), emission.as<float4>(), emitters.as<int>(), bv.nodes,
                     bv.tris, n_tris, n_emit, k_refill_lanes, k_trace_steps, nullptr, 0,
-                    bvh_width == 2 ? nullptr : bv.wide};
+                    bvh_width == 2 ? nullptr : bv.wide, bv.tri_nrm};
 }
 
 FrameParams Renderer::frame_params(uint32_t spp, uint32_t slots, uint32_t tiles_x) const {
