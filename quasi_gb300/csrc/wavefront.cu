@@ -10,6 +10,10 @@
 #include <cmath>
 #include <cstring>
 
+#ifndef QUASI_TRACE_L1_CARVEOUT
+#define QUASI_TRACE_L1_CARVEOUT 0
+#endif
+
 namespace quasi {
 
 // ---------------------------------------------------------------------------- host
@@ -397,6 +401,13 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
     const ClosestFn kc = closest_fns[opt_.collect_stats ? 1 : 0][mode];
     const ShadowFn ks = shadow_fns[opt_.collect_stats ? 1 : 0][mode];
     int occ_c = 0, occ_s = 0;
+#if QUASI_TRACE_L1_CARVEOUT
+    if (tree_smem == 0) {
+        // no shared memory in these kernels: leave the most of the unified L1 to the cache
+        cudaFuncSetAttribute(kc, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+        cudaFuncSetAttribute(ks, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+    }
+#endif
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, kc, tb, tree_smem);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, ks, tb, tree_smem);
     const int grid_c = sm_count_ * std::max(occ_c, 1);
