@@ -327,8 +327,9 @@ Q_CUDA_EXPORT int Q_cuda_backward(Q_plugin_handle* handle, const float* device_g
 
 /* Runs the autotuner on the current scene, frame size and options: times short frames
  * (at most 8 spp) of each candidate form (wavefront or megakernel), wave size, trace block
- * size and shared-memory treelet depth, keeps the fastest in the options (megakernel,
- * wave_spp, trace_block, smem_levels) and resets the accumulation. Needs a previous render
+ * size and refill threshold (8-wide records) or shared-memory treelet depth (binary LBVH),
+ * keeps the fastest in the options (megakernel, wave_spp, trace_block, refill_lanes or
+ * smem_levels) and resets the accumulation. Needs a previous render
  * (for the frame size). budget_ms bounds the time spent (0 = 2000 ms). */
 Q_CUDA_EXPORT int Q_cuda_autotune(Q_plugin_handle* handle, double budget_ms);
 

@@ -10,10 +10,6 @@
 #include <cmath>
 #include <cstring>
 
-#ifndef QUASI_TRACE_L1_CARVEOUT
-#define QUASI_TRACE_L1_CARVEOUT 0
-#endif
-
 namespace quasi {
 
 // ---------------------------------------------------------------------------- host
@@ -401,13 +397,6 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
     const ClosestFn kc = closest_fns[opt_.collect_stats ? 1 : 0][mode];
     const ShadowFn ks = shadow_fns[opt_.collect_stats ? 1 : 0][mode];
     int occ_c = 0, occ_s = 0;
-#if QUASI_TRACE_L1_CARVEOUT
-    if (tree_smem == 0) {
-        // no shared memory in these kernels: leave the most of the unified L1 to the cache
-        cudaFuncSetAttribute(kc, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
-        cudaFuncSetAttribute(ks, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
-    }
-#endif
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, kc, tb, tree_smem);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, ks, tb, tree_smem);
     const int grid_c = sm_count_ * std::max(occ_c, 1);
@@ -738,8 +727,9 @@ int Renderer::kernel_times(Q_cuda_kernel_time* out, uint32_t capacity, uint32_t*
     return QUASI_OK;
 }
 
-// Coordinate search over the renderer form, wave size, trace block size and treelet depth,
-// timing short progressive frames (at most 8 spp, LBVH kept) with the frame events.
+// Coordinate search over the renderer form, wave size, trace block size and the refill
+// threshold (8-wide records) or treelet depth (binary LBVH), timing short progressive frames
+// (at most 8 spp, LBVH kept) with the frame events.
 int Renderer::autotune(double budget_ms) {
     if (!has_scene_ || width_ == 0 || height_ == 0) return fail(QUASI_ERR_STATE, "render a frame before autotune");
     if (opt_.integrator != QUASI_INTEGRATOR_NEE) return fail(QUASI_ERR_STATE, "autotune needs the NEE integrator");
@@ -773,6 +763,8 @@ int Renderer::autotune(double budget_ms) {
         R_TRY(cudaEventElapsedTime(&ms, ev_frame0_, ev_frame1_), "event time");
         return QUASI_OK;
     };
+    // the last dimension: refill threshold for the 8-wide records, treelet depth for the binary
+    const bool wide = base.bvh_width != 2;
     Q_cuda_options best = base;
     float best_ms = 0.f;
     int rc = measure(best, best_ms);
@@ -784,15 +776,20 @@ int Renderer::autotune(double budget_ms) {
         std::vector<uint32_t> vals;
         if (dim == 0) vals = {0u, 1u};
         if (dim == 1)
-            for (uint32_t target : {2u << 20, 4u << 20, 8u << 20, 16u << 20})
+            for (uint32_t target : {8u << 20, 16u << 20, 32u << 20, 64u << 20})
                 vals.push_back(std::max<uint32_t>(1, std::min<uint32_t>(base.spp_per_frame, target / slots)));
         if (dim == 2) vals = {64u, 128u, 256u};
-        if (dim == 3) vals = {0u, 7u, 32u};
+        if (dim == 3) vals = wide ? std::vector<uint32_t>{2u, 4u, 8u} : std::vector<uint32_t>{0u, 7u, 32u};
         for (uint32_t v : vals) {
             if (elapsed() >= budget_ms) break;
             Q_cuda_options o = best;
-            uint32_t& field = dim == 0 ? o.megakernel : dim == 1 ? o.wave_spp : dim == 2 ? o.trace_block : o.smem_levels;
+            uint32_t& field = dim == 0   ? o.megakernel
+                              : dim == 1 ? o.wave_spp
+                              : dim == 2 ? o.trace_block
+                              : wide     ? o.refill_lanes
+                                         : o.smem_levels;
             if (field == v || (dim == 2 && field == 0 && v == 128)) continue;
+            if (dim == 3 && wide && field == 0 && v == static_cast<uint32_t>(k_wide_refill_lanes)) continue;
             if (dim == 2 && o.megakernel) continue;  // the megakernel runs 128-thread blocks
             if (dim == 3 && o.megakernel) continue;
             field = v;
@@ -813,6 +810,7 @@ int Renderer::autotune(double budget_ms) {
     opt_.wave_spp = best.wave_spp;
     opt_.trace_block = best.trace_block;
     opt_.smem_levels = best.smem_levels;
+    opt_.refill_lanes = best.refill_lanes;
     prof_.set_enabled(opt_.profile != 0);
     bvh_dirty_ = true;  // the treelet depth may have changed
     return reset();

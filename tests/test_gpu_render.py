@@ -243,6 +243,7 @@ def test_autotune_keeps_images(cuda_ok):
     h.autotune(1500)
     o = h.options()
     assert o.megakernel in (0, 1) and o.trace_block in (0, 64, 128, 256) and o.smem_levels in (0, 7, 32)
+    assert o.refill_lanes in (0, 2, 4, 8)
     assert o.spp_per_frame == 16 and o.max_depth == 6 and o.wave_spp in (1, 2, 4, 8, 16)
     h.render(160, 96)
     assert np.array_equal(h.readback(), ref)
