@@ -221,7 +221,12 @@ int BatchRenderer::upload_table() {
 // Cuts every scene's frame (min(spp, spp_cap) samples) into items of whole sample planes and
 // packs them into waves of at most W path slots, scene after scene.
 int BatchRenderer::plan(uint32_t spp_cap) {
-    uint32_t W = opt_.wave_paths ? opt_.wave_paths : k_default_wave_paths;
+    // per path slot: two ray queues (2 x 32), hit 16, shadow ray 48, beta, radiance and two
+    // AOVs (4 x 16), double-float ray 48, (scene, local path) 8
+    constexpr size_t bytes_per_path = 248;
+    uint32_t W = opt_.wave_paths ? opt_.wave_paths
+                                 : static_cast<uint32_t>(wave_paths_fitting(k_default_wave_paths, bytes_per_path,
+                                                                            size_t(wave_capacity_) * bytes_per_path));
     W = std::max(W, max_slots_);
     items_host_.clear();
     waves_.clear();

@@ -13,6 +13,22 @@
 
 namespace quasi {
 
+// Path slots of a wave that fit in device memory: at most `want`, leaving a sixteenth of
+// the device free; `held` is what the wave buffers already occupy (freed when they grow).
+// A device with less free memory gets smaller waves (slower, same images) instead of an
+// allocation failure.
+inline uint64_t wave_paths_fitting(uint64_t want, size_t bytes_per_path, size_t held) {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        return want;
+    }
+    const size_t margin = total_b / 16;
+    const size_t avail = free_b + held > margin ? free_b + held - margin : 0;
+    const uint64_t fit = avail / bytes_per_path;
+    return fit < want ? fit : want;
+}
+
 // NVTX range over a host scope (frame, LBVH build, wave): lets a profiler attribute and
 // filter the launches inside it (ncu --nvtx --nvtx-include "quasi.wave/"). Without an
 // attached tool the calls return at once.

@@ -246,6 +246,10 @@ int Renderer::ensure_frame_buffers(uint32_t w, uint32_t h) {
     return reset();
 }
 
+// Bytes of wave state per path slot: two ray queues (2 x 32), hit 16, shadow ray 48, beta,
+// radiance and two AOVs (4 x 16), signature 4, double-float ray 48.
+constexpr size_t k_wave_bytes_per_path = 244;
+
 int Renderer::ensure_wave_buffers(uint32_t paths) {
     if (paths <= wave_capacity_) return QUASI_OK;
     R_TRY(queue_[0].reserve(sizeof(float4) * 2ull * paths), "queue");
@@ -270,8 +274,9 @@ uint32_t Renderer::effective_wave_spp(uint32_t spp) const {
     // end, and larger waves keep those queues long enough to fill the GPU (1080p, 64 spp on
     // the 1M soup: 2 spp per wave 885, 4 spp 971, 8 spp 1024, 16 spp 1053, 32 spp 1071,
     // 64 spp 1080 Mrays/s on GB300)
-    const uint32_t target = 64u << 20;
-    return std::max<uint32_t>(1, std::min<uint32_t>(spp, target / std::max<uint32_t>(slots, 1)));
+    const uint64_t target = wave_paths_fitting(64u << 20, k_wave_bytes_per_path,
+                                               size_t(wave_capacity_) * k_wave_bytes_per_path);
+    return std::max<uint32_t>(1, static_cast<uint32_t>(std::min<uint64_t>(spp, target / std::max<uint32_t>(slots, 1))));
 }
 
 int Renderer::render(const Q_render_frame& fr) {

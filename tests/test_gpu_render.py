@@ -4,8 +4,8 @@ Tolerance: per-pixel relative error |gpu - oracle| / max(|oracle|, 1e-3) <= 1e-4
 pixel whose path signatures (the sequence of triangles hit and shadow-ray outcomes) all
 agree with the oracle's, and the same bound per sample. A path whose FP32 traversal decision
 differs from FP64 (a ray within ~1e-7 of a triangle edge) is counted as divergent; at most
-2 pixels in 10,000 may contain one (measured: 2 divergent samples of 1,048,576 on the
-256x256x16 Cornell box).
+2 pixels in 10,000 may contain one, or 2 pixels on images under 10,000 pixels (measured: 2
+divergent samples of 1,048,576 on the 256x256x16 Cornell box).
 """
 from __future__ import annotations
 
@@ -54,7 +54,8 @@ def _check_parity(img, rad, sig, ref, w, h, spp, max_divergent=2e-4):
     px_ok = match.all(-1)
     p_err = _rel(img[..., :3].astype(np.float64), ref["mean"].reshape(h, w, 3)).max(-1)
     assert p_err[px_ok].max() <= REL_TOL, p_err[px_ok].max()
-    assert 1.0 - px_ok.mean() <= max_divergent, 1.0 - px_ok.mean()
+    # at most max_divergent of the pixels, and at least 2 pixels on small images
+    assert (~px_ok).sum() <= max(max_divergent * px_ok.size, 2), (~px_ok).sum()
     return p_err, px_ok
 
 
@@ -271,3 +272,52 @@ def test_wide_and_binary_traversal_agree(host, spec, w, h, spp, depth):
         if same.all():
             assert np.array_equal(img8, img2), key
     host.set_options(bvh_width=0, megakernel=0)
+
+
+def _edge_scene(kind: str) -> q.Scene:
+    rng = np.random.default_rng(21)
+    cam = {"position": (0.5, 0.5, -1.0), "target": (0.5, 0.5, 0.5), "fov": 40.0}
+    if kind == "empty":
+        v = np.zeros((0, 9), np.float32)
+    elif kind == "one_emitter":
+        v = np.array([[0.1, 0.1, 0.5, 0.9, 0.1, 0.5, 0.5, 0.9, 0.5]], np.float32)
+    elif kind == "two":
+        v = np.array([[0.1, 0.1, 0.5, 0.9, 0.1, 0.5, 0.5, 0.9, 0.5],
+                      [0.0, 0.0, 0.2, 1.0, 0.0, 0.2, 0.5, 0.0, 1.0]], np.float32)
+    elif kind == "no_emitters":
+        v = (rng.random((400, 9)) * 0.8 + 0.1).astype(np.float32)
+    else:  # "degenerate": a soup with zero-area triangles (a vertex repeated), some emitting
+        v = (rng.random((500, 9)) * 0.8 + 0.1).astype(np.float32)
+        v[::7, 3:6] = v[::7, 0:3]
+        v[1::11, 6:9] = v[1::11, 3:6]
+    n = v.shape[0]
+    albedo = np.full((n, 3), 0.6, np.float32)
+    emission = np.zeros((n, 3), np.float32)
+    if kind in ("one_emitter", "two"):
+        emission[0] = (5.0, 4.0, 3.0)
+    if kind == "degenerate":
+        emission[::9] = (3.0, 3.0, 3.0)
+    return q.Scene(v, albedo, emission, cam)
+
+
+@pytest.mark.parametrize("kind,w,h,spp,depth", [("empty", 16, 8, 2, 4), ("one_emitter", 37, 23, 4, 1),
+                                                 ("two", 37, 23, 4, 3), ("no_emitters", 24, 20, 2, 4),
+                                                 ("degenerate", 40, 28, 4, 5)])
+def test_edge_scenes_parity(host, orc, kind, w, h, spp, depth):
+    """Empty and tiny scenes, a scene without emitters, zero-area triangles, image sizes that
+    are not multiples of the 8x4 pixel tile, and depth 1: parity with the FP64 oracle."""
+    scene = _edge_scene(kind)
+    img, rad, sig, st = _render(host, scene, w, h, spp, depth, seed=4)
+    ref = orc.render_nee(scene, w, h, spp, depth, seed=4, camera=scene.camera, want_samples=True)
+    _check_parity(img, rad, sig, ref, w, h, spp)
+    assert st.camera_rays == w * h * spp
+    if kind in ("empty", "no_emitters"):
+        assert np.all(img[..., :3] == 0.0) and st.shadow_rays == 0
+
+
+def test_options_and_frames_are_validated(host):
+    host.set_scene(q.make_scene("cornell36", host.lib))
+    for bad in (dict(bvh_width=4), dict(refill_lanes=33), dict(trace_block=48), dict(max_depth=65)):
+        with pytest.raises(q.QuasiError):
+            host.set_options(**bad)
+    host.set_options(bvh_width=0, refill_lanes=0, trace_block=0, max_depth=4)
