@@ -208,13 +208,14 @@ __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, cons
     }
     const int refs[8] = {w4.x, w4.y, w4.z, w4.w, w5.x, w5.y, w5.z, w5.w};
     uint32_t im = mask_xor_permute(hit & imask, q.oct);
-    uint32_t lm = mask_xor_permute(hit & ~imask, q.oct);
-    // leaves first: a hit found here shortens every interval tested after it
+    // leaves first: a hit found here shortens every interval tested after it. Every leaf hit
+    // is tested (no culling by entry distance) and the closest-hit rule does not depend on
+    // the order, so they go in slot order, without the rank permutation.
+    uint32_t lm = hit & ~imask;
     while (lm) {
-        const uint32_t p = 31u - __clz(lm);
-        lm &= ~(1u << p);
-        if (wide_leaf<ANY, STATS>(tris, r, sel8(refs, p ^ q.oct), q.tmax, q.exclude, q.best_t, q.best, q.bu, q.bv,
-                                  cnt)) {
+        const uint32_t s = __ffs(lm) - 1;
+        lm &= lm - 1u;
+        if (wide_leaf<ANY, STATS>(tris, r, sel8(refs, s), q.tmax, q.exclude, q.best_t, q.best, q.bu, q.bv, cnt)) {
             q.node = k_wide_done;
             return true;
         }
