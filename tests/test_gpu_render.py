@@ -321,3 +321,31 @@ def test_options_and_frames_are_validated(host):
         with pytest.raises(q.QuasiError):
             host.set_options(**bad)
     host.set_options(bvh_width=0, refill_lanes=0, trace_block=0, max_depth=4)
+
+
+def test_benchmark_frame_parity_sampled_pixels(orc):
+    """The benchmark configuration itself: 1M-triangle soup, 1920x1080, 64 spp, depth 8, LBVH
+    built on the GPU. Every sample of 200 random pixels against the FP64 oracle (per-sample
+    and per-pixel relative error <= 1e-4 on agreeing paths)."""
+    w, h, spp, depth = 1920, 1080, 64, 8
+    host = q.PluginHost(width=w, height=h)
+    scene = q.make_scene("soup:n=1000000,seed=0", host.lib)
+    host.set_scene(scene)
+    host.set_options(spp_per_frame=spp, max_depth=depth, seed=17, record_samples=1)
+    host.render(w, h, dirty=True)
+    img = host.readback()
+    rad, sig = host.read_samples(spp)
+    st = host.stats()
+    host.destroy()
+    assert st.error_flags == 0
+    rng = np.random.default_rng(3)
+    pix = rng.choice(w * h, size=200, replace=False).astype(np.uint32)
+    ref = orc.render_nee(scene, w, h, spp, depth, seed=17, pixels=pix, want_samples=True)
+    ys, xs = pix // w, pix % w
+    match = sig[ys, xs] == ref["sig"]
+    assert match.mean() >= 0.999, match.mean()
+    assert _rel(rad[ys, xs].astype(np.float64), ref["samples"]).max(-1)[match].max() <= REL_TOL
+    px_ok = match.all(-1)
+    p_err = _rel(img[ys, xs, :3].astype(np.float64), ref["mean"]).max(-1)
+    assert p_err[px_ok].max() <= REL_TOL, p_err[px_ok].max()
+    assert (~px_ok).sum() <= 2
