@@ -59,6 +59,26 @@ __device__ __forceinline__ ff3 tri_unit_normal(const float4* __restrict__ tri_nr
 // hit: (t, prim, u, v) from the FP32 traversal; ro, rd: the double-float ray that found it.
 __device__ __forceinline__ void shade_vertex(const VertexScene& s, uint32_t key, int prim, float4 hit, const ff3& ro,
                                              const ff3& rd, bool want_dir, VertexResult& out) {
+    // The light choice depends only on the path key: start its dependent loads (emitter
+    // index, then the light triangle and its table entry) before the hit-point arithmetic so
+    // their latency overlaps it.
+    uint32_t st = key;
+    const uint32_t sel = pcg_hash(st);
+    st = sel;
+    const float r1 = rng_next(st);
+    const float r2 = rng_next(st);
+    int l = -1;
+    float4 lv0 = make_float4(0.f, 0.f, 0.f, 0.f), lv1 = lv0, lv2 = lv0, ln0 = lv0, ln1 = lv0;
+    if (s.n_emit > 0) {
+        l = __ldg(&s.emitters[static_cast<uint32_t>((static_cast<uint64_t>(sel) * s.n_emit) >> 32)]);
+        if (l != prim) {
+            lv0 = __ldg(&s.tri_in[3 * l]);
+            lv1 = __ldg(&s.tri_in[3 * l + 1]);
+            lv2 = __ldg(&s.tri_in[3 * l + 2]);
+            ln0 = __ldg(&s.tri_nrm[2 * l]);
+            ln1 = __ldg(&s.tri_nrm[2 * l + 1]);
+        }
+    }
     const float3 a = xyz(__ldg(&s.tri_in[3 * prim]));
     ff area_h;
     ff3 nrm = tri_unit_normal(s.tri_nrm, prim, area_h);
@@ -74,21 +94,15 @@ __device__ __forceinline__ void shade_vertex(const VertexScene& s, uint32_t key,
     }
     if (den.hi > 0.0f) nrm = ff3_neg(nrm);
     out.nrm = ff3_f(nrm);
-    uint32_t st = key;
-    const uint32_t sel = pcg_hash(st);
-    st = sel;
-    const float r1 = rng_next(st);
-    const float r2 = rng_next(st);
     out.org = ff3_add(x, ff3_scale(nrm, s.eps));
     out.nee = false;
     out.light = -1;
     out.g = 0.0f;
     if (s.n_emit > 0) {
-        const int l = __ldg(&s.emitters[static_cast<uint32_t>((static_cast<uint64_t>(sel) * s.n_emit) >> 32)]);
         if (l != prim) {
-            const float3 la = xyz(__ldg(&s.tri_in[3 * l]));
-            const ff3 le1 = ff3_diff(xyz(__ldg(&s.tri_in[3 * l + 1])), la);
-            const ff3 le2 = ff3_diff(xyz(__ldg(&s.tri_in[3 * l + 2])), la);
+            const float3 la = xyz(lv0);
+            const ff3 le1 = ff3_diff(xyz(lv1), la);
+            const ff3 le2 = ff3_diff(xyz(lv2), la);
             const ff su = ff_sqrt(ffv(r1));
             const ff3 yl = ff3_add(ff3_add(ff3v(la), ff3_scale(le1, ff_mul(su, two_sum(1.0f, -r2)))),
                                    ff3_scale(le2, ff_mul(su, r2)));
@@ -102,8 +116,8 @@ __device__ __forceinline__ void shade_vertex(const VertexScene& s, uint32_t key,
             const float inv_dist = __fdiv_rn(1.0f, __fsqrt_rn(d2));
             const float3 wi = mk3(__fmul_rn(dv.x, inv_dist), __fmul_rn(dv.y, inv_dist), __fmul_rn(dv.z, inv_dist));
             const float cos_x = fdot3(ff3_f(nrm), wi);
-            ff area2;
-            const ff3 nl = tri_unit_normal(s.tri_nrm, l, area2);
+            const ff area2 = ff{ln1.z, ln1.w};
+            const ff3 nl = ff3{ff{ln0.x, ln0.y}, ff{ln0.z, ln0.w}, ff{ln1.x, ln1.y}};
             const float cl = fdot3(ff3_f(nl), wi);
             const float cos_l = fabsf(cl);
             if (cos_x > 0.0f && cos_l > 0.0f && d2 > 0.0f) {
