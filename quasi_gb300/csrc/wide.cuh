@@ -46,8 +46,9 @@ constexpr int k_wide_node_f4 = 6;     // float4 per wide record
 constexpr int k_wide_empty_ref = ~3;  // leaf with code 3: no triangles
 // Minimum resident 256-thread blocks per SM asked of the compiler for the 8-wide trace
 // kernels, a register cap (4 -> 64 registers per thread). Uncapped, they take 93 registers
-// and 5 blocks of 128 threads fit an SM; at 64 registers (a few bytes of spills) 8 fit, and
-// the 1M-triangle frame renders 18% faster on GB300.
+// and 5 blocks of 128 threads fit an SM; at 64 registers (no spills) 8 fit, and the
+// 1M-triangle frame renders 18% faster on GB300. Tighter caps spill: 56 registers (9 blocks
+// of 128) cost 3%, 51 (10 blocks) 11%.
 #ifndef QUASI_WIDE_MIN_BLOCKS
 #define QUASI_WIDE_MIN_BLOCKS 4
 #endif
