@@ -258,12 +258,17 @@ def test_wide_and_binary_traversal_agree(host, spec, w, h, spp, depth):
     to the lower triangle index) and the same shadow-ray outcomes: both forms give the same
     path signatures and the same radiance bits, in the wavefront and the megakernel."""
     scene = q.make_scene(spec, host.lib)
+    # (bvh_width, megakernel, refill_lanes, smem_levels): binary with a shared-memory treelet,
+    # binary with per-lane refill, binary without treelet, 8-wide with refill (default),
+    # 8-wide whole-warp batches, megakernel
+    forms = ((2, 0, 0, 0), (2, 0, 8, 0), (2, 0, 0, 32), (8, 0, 0, 0), (8, 0, 32, 0), (8, 1, 0, 0))
     out = {}
-    for width, mega in ((2, 0), (8, 0), (8, 1)):
-        img, rad, sig, st = _render(host, scene, w, h, spp, depth, seed=11, bvh_width=width, megakernel=mega)
-        out[(width, mega)] = (img, rad, sig, st)
-    img2, rad2, sig2, st2 = out[(2, 0)]
-    for key in ((8, 0), (8, 1)):
+    for width, mega, refill, levels in forms:
+        img, rad, sig, st = _render(host, scene, w, h, spp, depth, seed=11, bvh_width=width, megakernel=mega,
+                                    refill_lanes=refill, smem_levels=levels)
+        out[(width, mega, refill, levels)] = (img, rad, sig, st)
+    img2, rad2, sig2, st2 = out[forms[0]]
+    for key in forms[1:]:
         img8, rad8, sig8, st8 = out[key]
         same = sig8 == sig2
         assert same.mean() >= 1.0 - 1e-5, (key, same.mean())
@@ -271,7 +276,7 @@ def test_wide_and_binary_traversal_agree(host, spec, w, h, spp, depth):
         assert st8.camera_rays == st2.camera_rays
         if same.all():
             assert np.array_equal(img8, img2), key
-    host.set_options(bvh_width=0, megakernel=0)
+    host.set_options(bvh_width=0, megakernel=0, refill_lanes=0, smem_levels=0)
 
 
 def _edge_scene(kind: str) -> q.Scene:
