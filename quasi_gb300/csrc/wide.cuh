@@ -237,7 +237,8 @@ __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, cons
         // Any-hit: visit next the internal child whose box covers the longest stretch of the
         // segment (where an occluder is likeliest), push the others lowest rank first. On
         // occluded shadow segments through the 1M soup this visits 17% fewer records than
-        // nearest-first.
+        // nearest-first. Also stacking the runner-up on top saved 3% more visits but its
+        // bookkeeping in the eight-child loop cost more (frame 1% slower).
         next = sel8(refs, best_slot);
         im &= ~(1u << (best_slot ^ q.oct));
         while (im) {
