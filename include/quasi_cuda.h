@@ -186,19 +186,21 @@ typedef struct Q_cuda_options {
     uint32_t seed;               /* RNG seed (0) */
     uint32_t integrator;         /* QUASI_INTEGRATOR_* */
     uint32_t rebuild_each_frame; /* rebuild the LBVH in every frame (1 = yes) */
-    uint32_t wave_spp;           /* samples per pixel per wavefront (0 = autotuned) */
+    uint32_t wave_spp;           /* samples per pixel per wavefront (0 = as many as fit ~64M
+                                    path slots, fewer if free device memory is short) */
     uint32_t trace_block;        /* threads per block of the trace kernels (0 = auto) */
     uint32_t record_samples;     /* keep per-sample radiance and path signatures */
     uint32_t collect_stats;      /* count BVH node visits and triangle tests */
     uint32_t profile;            /* time every kernel launch with CUDA events */
     uint32_t megakernel;         /* 1 = one-kernel path tracer instead of the wavefront */
-    uint32_t smem_levels;        /* top BVH levels staged in shared memory per block
-                                    (0 = default 5, 1..9, 32 = none) */
+    uint32_t smem_levels;        /* binary LBVH only: top levels staged in shared memory per
+                                    block (0 = default 5, 1..9, 32 = none) */
     float ray_eps;               /* ray origin offset along the normal (1e-4) */
     uint32_t refill_lanes;       /* trace kernels refill a warp once this many lanes idle
                                     (1..32; 32 = refill only whole warps; 0 = default:
                                     4 for the 8-wide records, 32 for the binary LBVH) */
-    uint32_t trace_steps;        /* node visits per lane between refill checks (0 = default) */
+    uint32_t trace_steps;        /* binary LBVH with refill only: node visits per lane
+                                    between refill checks (0 = default) */
     uint32_t bvh_width;          /* traversal structure: 8 = 8-wide records collapsed from the
                                     LBVH (default, 0), 2 = the binary LBVH nodes */
 } Q_cuda_options;
