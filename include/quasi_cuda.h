@@ -188,7 +188,7 @@ typedef struct Q_cuda_options {
     uint32_t rebuild_each_frame; /* rebuild the LBVH in every frame (1 = yes) */
     uint32_t wave_spp;           /* samples per pixel per wavefront (0 = as many as fit ~64M
                                     path slots, fewer if free device memory is short) */
-    uint32_t trace_block;        /* threads per block of the trace kernels (0 = auto) */
+    uint32_t trace_block;        /* threads per block of the trace kernels (0 = 256 over the 8-wide records, 128 binary) */
     uint32_t record_samples;     /* keep per-sample radiance and path signatures */
     uint32_t collect_stats;      /* count BVH node visits and triangle tests */
     uint32_t profile;            /* time every kernel launch with CUDA events */

@@ -301,8 +301,10 @@ void BatchRenderer::compute_grids() {
     auto km = stats ? k_batch_megakernel<true> : k_batch_megakernel<false>;
     const int tb = static_cast<int>(opt_.trace_block), mb = std::min(tb, 128);
     int occ_c = 0, occ_s = 0, occ_m = 0, occ_a = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, kc, tb, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, ks, tb, 0);
+    smem_c_ = wide ? wide_stack_smem_bytes<false>(tb) : 0;
+    smem_s_ = wide ? wide_stack_smem_bytes<true>(tb) : 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, kc, tb, smem_c_);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, ks, tb, smem_s_);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_m, km, mb, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, k_batch_adjoint, 128, 0);
     const int sm = owner_.sm_count();
@@ -364,7 +366,7 @@ int BatchRenderer::record_frame(cudaStream_t s, uint32_t& launches) {
                 int* f_cur = cnt + 2 * D + (k - 1);
                 int* f_shadow = cnt + 3 * D + (k - 1);
                 B_TRY(QUASI_LAUNCH(prof_, "batch_trace_closest", s,
-                                   (kc<<<grid_c, tb, 0, s>>>(table, meta, qcur, hits_.as<float4>(), c_cur, cap, chunk,
+                                   (kc<<<grid_c, tb, smem_c_, s>>>(table, meta, qcur, hits_.as<float4>(), c_cur, cap, chunk,
                                                              refill, f_cur, err, st))),
                       "batch_trace_closest");
                 B_TRY(QUASI_LAUNCH(prof_, "batch_shade", s,
@@ -373,7 +375,7 @@ int BatchRenderer::record_frame(cudaStream_t s, uint32_t& launches) {
                                                                              shadow_.as<float4>(), c_shadow))),
                       "batch_shade");
                 B_TRY(QUASI_LAUNCH(prof_, "batch_trace_shadow", s,
-                                   (ks<<<grid_s, tb, 0, s>>>(table, meta, pd, shadow_.as<float4>(), c_shadow, cap, chunk,
+                                   (ks<<<grid_s, tb, smem_s_, s>>>(table, meta, pd, shadow_.as<float4>(), c_shadow, cap, chunk,
                                                              refill, f_shadow, err, st))),
                       "batch_trace_shadow");
             }

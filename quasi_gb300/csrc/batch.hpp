@@ -99,6 +99,7 @@ private:
     uint32_t kernels_per_frame_ = 0;
     uint64_t frames_since_reset_ = 0;
     int grid_c_ = 0, grid_s_ = 0, grid_m_ = 0, grid_adj_ = 0;  // persistent grids (SMs x occupancy)
+    size_t smem_c_ = 0, smem_s_ = 0;  // dynamic shared memory of a trace block (8-wide stacks)
 
     cudaStream_t capture_ = nullptr;
     cudaGraphExec_t frame_exec_ = nullptr, adjoint_exec_ = nullptr;

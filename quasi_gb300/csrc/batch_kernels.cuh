@@ -115,14 +115,16 @@ __device__ __forceinline__ void trace_batches_multi(Job& job, const BatchSceneDe
 
 // Persistent traversal over rays of several scenes with per-lane refill on the 8-wide
 // records: once `refill` lanes of a warp are idle they take the next rays with one atomic;
-// each lane traverses the records of its own ray's scene.
+// each lane traverses the records of its own ray's scene. Blocks are launched with
+// wide_stack_smem_bytes<ANY>(blockDim.x) of dynamic shared memory (the stacks' shared part).
 template <bool ANY, bool STATS, class Job>
 __device__ __forceinline__ void trace_wide_refill_multi(Job& job, const BatchSceneDev* __restrict__ scenes,
                                                         const uint2* __restrict__ meta, int n, int refill,
                                                         int* __restrict__ fetch, uint32_t& err, TraceCounters& cnt) {
     const int lane = threadIdx.x & 31;
     WideRay q;
-    int2 stack[k_wide_stack];
+    WideStack<wide_smem_stack<ANY>()> stack;
+    stack.slot = wide_stack_slot<ANY>();
     const float4* wide = nullptr;
     const float4* tris = nullptr;
     bool active = false, exhausted = false;

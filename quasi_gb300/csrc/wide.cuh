@@ -53,6 +53,64 @@ constexpr int k_wide_empty_ref = ~3;  // leaf with code 3: no triangles
 #define QUASI_WIDE_MIN_BLOCKS 4
 #endif
 
+// Stack entries per ray that the refill traversal keeps in shared memory, for closest-hit
+// and for any-hit rays; deeper entries go to a thread-local array. Local-memory stack
+// traffic shares L1 with the records, and a pop is a dependent load before the next record
+// fetch. On the 1M soup 99% of rays never stack more than 15 entries. Measured per frame
+// (1080p, 64 spp, 128-thread blocks), closest-hit kernel time by entries: none 334.6 ms,
+// 10: 317.3, 12: 314.1, 16: 310.4, 20: 312.9; any-hit: none 142.4, 10: 138.7, 12: 136.0,
+// 16: 130.7, 20: 128.0, 24: 134.9 (deeper shared stacks take L1 capacity the records use).
+// With 16 and 20 the frame renders at 1389 Mrays/s against 1289 with local stacks only.
+#ifndef QUASI_WIDE_SMEM_STACK
+#define QUASI_WIDE_SMEM_STACK 16
+#endif
+#ifndef QUASI_WIDE_SMEM_STACK_ANY
+#define QUASI_WIDE_SMEM_STACK_ANY 20
+#endif
+template <bool ANY>
+__host__ __device__ constexpr int wide_smem_stack() {
+    return ANY ? QUASI_WIDE_SMEM_STACK_ANY : QUASI_WIDE_SMEM_STACK;
+}
+static_assert(wide_smem_stack<false>() >= 0 && wide_smem_stack<false>() <= k_wide_stack &&
+                  wide_smem_stack<true>() >= 0 && wide_smem_stack<true>() <= k_wide_stack,
+              "shared stack entries");
+static_assert(sizeof(int2) * wide_smem_stack<false>() * 256 <= 48 * 1024 &&
+                  sizeof(int2) * wide_smem_stack<true>() * 256 <= 48 * 1024,
+              "a 256-thread trace block stays within the default dynamic shared memory limit");
+
+// Dynamic shared memory a refill trace block of `threads` threads needs for its stacks.
+template <bool ANY>
+constexpr size_t wide_stack_smem_bytes(int threads) {
+    return sizeof(int2) * static_cast<size_t>(wide_smem_stack<ANY>()) * static_cast<size_t>(threads);
+}
+
+// Traversal stack of one ray: entries below Sh in shared memory, warp-major (entry i of a
+// lane at slot[32 i], so the lanes of a warp touch 32 consecutive int2 whatever their
+// depths: no bank conflicts), the rest in a thread-local array.
+template <int Sh>
+struct WideStack {
+    int2* slot;
+    int2 loc[k_wide_stack - Sh];
+    __device__ __forceinline__ void put(int i, int2 e) {
+        if (Sh > 0 && i < Sh)
+            slot[32 * i] = e;
+        else
+            loc[i - Sh] = e;
+    }
+    __device__ __forceinline__ int2 get(int i) const {
+        if (Sh > 0 && i < Sh) return slot[32 * i];
+        return loc[i - Sh];
+    }
+};
+
+// This thread's shared slots in a block launched with wide_stack_smem_bytes<ANY>(blockDim.x)
+// of dynamic shared memory.
+template <bool ANY>
+__device__ __forceinline__ int2* wide_stack_slot() {
+    extern __shared__ int2 s_wide_stack[];
+    return s_wide_stack + (threadIdx.x >> 5) * (32 * wide_smem_stack<ANY>()) + (threadIdx.x & 31);
+}
+
 // Marks a finished traversal in WideRay::node (no record index is negative).
 constexpr int k_wide_done = static_cast<int>(0x80000000u);
 
@@ -76,8 +134,30 @@ __device__ __forceinline__ uint32_t mask_xor_permute(uint32_t m, uint32_t oct) {
     return m;
 }
 
-__device__ __forceinline__ float byte_f(uint32_t w, int k) {
-    return static_cast<float>((w >> (8 * k)) & 0xffu);
+// Byte k of w as the float 2^23 + byte: one byte permute into the mantissa of 2^23, exact.
+__device__ __forceinline__ float byte_f23(uint32_t w, int k) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7650u | static_cast<uint32_t>(k)));
+}
+
+// Two FP32 lanes in one 64-bit register and the paired arithmetic of sm_100 and later
+// (sub/fma .rn.f32x2): each lane rounds exactly as the scalar instruction does.
+__device__ __forceinline__ uint64_t f2_pack(float lo, float hi) {
+    uint64_t d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+    return d;
+}
+__device__ __forceinline__ void f2_unpack(uint64_t v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ uint64_t f2_sub(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
 }
 
 // Three-input minimum and maximum (one instruction each on sm_100 and later).
@@ -147,9 +227,10 @@ __device__ __forceinline__ void wide_begin(WideRay& q, float3 o, float3 d, float
 }
 
 // Pops the nearest stacked entry still closer than the best hit, or k_wide_done.
-__device__ __forceinline__ int wide_pop(WideRay& q, const int2* stack) {
+template <class Stack>
+__device__ __forceinline__ int wide_pop(WideRay& q, const Stack& stack) {
     while (q.sp > 0) {
-        const int2 e = stack[--q.sp];
+        const int2 e = stack.get(--q.sp);
         if (__int_as_float(e.y) < q.best_t) return e.x;
     }
     return k_wide_done;
@@ -161,9 +242,9 @@ __device__ __forceinline__ int wide_pop(WideRay& q, const int2* stack) {
 // visit and stacking the other leaves (each loop turn then costs one triangle test, not the
 // busiest lane's count) was measured 7% slower on the 1M soup: the extra stack traffic and
 // loop turns cost more than the divergence they remove.
-template <bool ANY, bool STATS>
+template <bool ANY, bool STATS, class Stack>
 __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, const float4* __restrict__ tris,
-                                           WideRay& q, int2* stack, uint32_t& err, TraceCounters& cnt) {
+                                           WideRay& q, Stack& stack, uint32_t& err, TraceCounters& cnt) {
     if (q.node == k_wide_done) return true;
     if (--q.budget == 0u) {
         err |= k_deverr_traversal;
@@ -182,8 +263,9 @@ __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, cons
     const float sy = __uint_as_float(((hdr >> 8) & 0xffu) << 23);
     const float sz = __uint_as_float(((hdr >> 16) & 0xffu) << 23);
     const uint32_t imask = hdr >> 24;
-    const float ax = sx * r.inv.x, ay = sy * r.inv.y, az = sz * r.inv.z;
-    const float bx = (w0.x - r.o.x) * r.inv.x, by = (w0.y - r.o.y) * r.inv.y, bz = (w0.z - r.o.z) * r.inv.z;
+    const float az = sz * r.inv.z, bz = (w0.z - r.o.z) * r.inv.z;
+    const uint64_t axy = f2_pack(sx * r.inv.x, sy * r.inv.y);
+    const uint64_t bxy = f2_pack((w0.x - r.o.x) * r.inv.x, (w0.y - r.o.y) * r.inv.y);
     // near planes are the lower ones along a positive direction component
     const uint32_t wx[4] = {__float_as_uint(w1.x), __float_as_uint(w1.y), __float_as_uint(w1.z), __float_as_uint(w1.w)};
     const uint32_t wy[4] = {__float_as_uint(w2.x), __float_as_uint(w2.y), __float_as_uint(w2.z), __float_as_uint(w2.w)};
@@ -202,9 +284,15 @@ __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, cons
         const uint32_t nyw = k < 4 ? ny0 : ny1, fyw = k < 4 ? fy0 : fy1;
         const uint32_t nzw = k < 4 ? nz0 : nz1, fzw = k < 4 ? fz0 : fz1;
         const int b = k & 3;
-        const float tnx = fmaf(byte_f(nxw, b), ax, bx), tfx = fmaf(byte_f(fxw, b), ax, bx);
-        const float tny = fmaf(byte_f(nyw, b), ay, by), tfy = fmaf(byte_f(fyw, b), ay, by);
-        const float tnz = fmaf(byte_f(nzw, b), az, bz), tfz = fmaf(byte_f(fzw, b), az, bz);
+        // plane distance q * a + b with q = (2^23 + q) - 2^23 (exact), the x and y planes in
+        // the two lanes of one paired subtract and FMA, z alone: the same bits as
+        // fmaf(q, a, b) per plane, in fewer instructions than integer-to-float conversions
+        // (1288 vs 1281 Mrays/s on the 1M soup)
+        float tnx, tny, tfx, tfy;
+        const uint64_t c23 = 0x4B0000004B000000ull;  // (2^23, 2^23)
+        f2_unpack(f2_fma(f2_sub(f2_pack(byte_f23(nxw, b), byte_f23(nyw, b)), c23), axy, bxy), tnx, tny);
+        f2_unpack(f2_fma(f2_sub(f2_pack(byte_f23(fxw, b), byte_f23(fyw, b)), c23), axy, bxy), tfx, tfy);
+        const float tnz = fmaf(byte_f23(nzw, b) - 8388608.0f, az, bz), tfz = fmaf(byte_f23(fzw, b) - 8388608.0f, az, bz);
         const float tnear = fmax3(tnx, tny, fmaxf(tnz, 0.0f));
         const float tfar = fmin3(tfx, tfy, fminf(tfz, q.best_t));
         tn[k] = tnear;
@@ -250,7 +338,7 @@ __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, cons
                 q.node = k_wide_done;
                 return true;
             }
-            stack[q.sp++] = make_int2(sel8(refs, s), __float_as_int(sel8(tn, s)));
+            stack.put(q.sp++, make_int2(sel8(refs, s), __float_as_int(sel8(tn, s))));
         }
     }
     // internal children: push all but the first-ranked, lowest rank first
@@ -267,7 +355,7 @@ __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, cons
                 q.node = k_wide_done;
                 return true;
             }
-            stack[q.sp++] = make_int2(ref, __float_as_int(t));
+            stack.put(q.sp++, make_int2(ref, __float_as_int(t)));
         } else {
             next = ref;
         }
@@ -286,7 +374,7 @@ __device__ __forceinline__ int trace_wide(const float4* __restrict__ wide, const
                                           float& bu, float& bv, uint32_t& err, TraceCounters& cnt) {
     WideRay q;
     wide_begin(q, r.o, r.d, tmax, exclude, n_tris);
-    int2 stack[k_wide_stack];
+    WideStack<0> stack;
     while (!wide_visit<ANY, STATS>(wide, tris, q, stack, err, cnt)) {
     }
     t_out = q.best_t;
@@ -325,14 +413,16 @@ __device__ __forceinline__ void trace_batches_wide(Job& job, const float4* __res
 // Persistent traversal of a ray queue with per-lane refill: once `refill` lanes of a warp
 // are idle they take the next rays with one atomic, while the other lanes carry on with
 // their own rays (refill = 32 waits for the whole warp). Job as in trace_batches. Every
-// lane of the warp must call this (it uses full-warp votes).
+// lane of the warp must call this (it uses full-warp votes), and the block must be launched
+// with wide_stack_smem_bytes<ANY>(blockDim.x) of dynamic shared memory.
 template <bool ANY, bool STATS, class Job>
 __device__ __forceinline__ void trace_wide_refill(Job& job, const float4* __restrict__ wide,
                                                   const float4* __restrict__ tris, uint32_t n_tris, int n, int refill,
                                                   int* __restrict__ fetch, uint32_t& err, TraceCounters& cnt) {
     const int lane = threadIdx.x & 31;
     WideRay q;
-    int2 stack[k_wide_stack];
+    WideStack<wide_smem_stack<ANY>()> stack;
+    stack.slot = wide_stack_slot<ANY>();
     bool active = false, exhausted = false;
     int idx = 0;
     while (true) {

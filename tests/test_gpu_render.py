@@ -9,10 +9,13 @@ divergent samples of 1,048,576 on the 256x256x16 Cornell box).
 """
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 import pytest
 
 import quasi_gb300 as q
+from quasi_gb300 import _abi as A
 
 pytestmark = pytest.mark.gpu
 
@@ -326,6 +329,17 @@ def test_options_and_frames_are_validated(host):
         with pytest.raises(q.QuasiError):
             host.set_options(**bad)
     host.set_options(bvh_width=0, refill_lanes=0, trace_block=0, max_depth=4)
+    # frames: more than 2^26 pixels and a zero extent are refused with a message, and the
+    # next valid frame renders (the error is per call, not sticky)
+    with pytest.raises(q.QuasiError, match="too large"):
+        host.render(8193, 8193, dirty=True)
+    f = A.Q_render_frame()
+    f.width, f.height, f.camera = 0, 16, host.camera
+    host.lib.Q_plugin_render(host.handle, ctypes.byref(f))
+    assert b"zero-sized" in host.lib.Q_cuda_last_error(host.handle)
+    host.render(16, 16, dirty=True)
+    assert host.readback().shape == (16, 16, 4)
+    assert host.stats().error_flags == 0
 
 
 def test_benchmark_frame_parity_sampled_pixels(orc):
