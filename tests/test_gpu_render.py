@@ -323,6 +323,48 @@ def test_edge_scenes_parity(host, orc, kind, w, h, spp, depth):
         assert np.all(img[..., :3] == 0.0) and st.shadow_rays == 0
 
 
+def _needle_scene(n=20000, seed=4, width=0.01) -> q.Scene:
+    """Long thin triangles across the unit cube: their boxes are large and overlap along
+    every ray while the triangles themselves are rarely hit, so a ray stacks many subtrees
+    before a hit culls them. In a CPU model of the same 8-wide records (same camera) most
+    rays stack more than 20 entries at some point (up to ~37): past the shared-memory part
+    of the stacks (16 entries closest-hit, 20 any-hit) into the thread-local part."""
+    rng = np.random.default_rng(seed)
+    a = rng.random((n, 3)) * 0.9 + 0.05
+    b = rng.random((n, 3)) * 0.9 + 0.05
+    d = rng.normal(0.0, 1.0, (n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    v = np.concatenate([a, b, a + d * width], axis=1).astype(np.float32)
+    albedo = np.full((n, 3), 0.7, np.float32)
+    emission = np.zeros((n, 3), np.float32)
+    emission[::31] = (4.0, 3.5, 3.0)
+    cam = {"position": (0.5, 0.5, -1.0), "target": (0.5, 0.5, 0.5), "fov": 40.0}
+    return q.Scene(v, albedo, emission, cam)
+
+
+def test_deep_stacks_forms_agree_and_match_oracle(host, orc):
+    """Rays whose traversal stacks overflow the shared-memory part: the 8-wide refill kernels
+    (256- and 64-thread blocks, so two shared-memory layouts) return the same hits and shadow
+    outcomes as the binary LBVH, and the image matches the FP64 oracle."""
+    scene = _needle_scene()
+    w, h, spp, depth = 64, 48, 4, 4
+    out = {}
+    for width, tb in ((2, 0), (8, 0), (8, 64)):
+        out[(width, tb)] = _render(host, scene, w, h, spp, depth, seed=9, bvh_width=width, trace_block=tb)
+    _, rad2, sig2, st2 = out[(2, 0)]
+    for key in ((8, 0), (8, 64)):
+        _, rad8, sig8, st8 = out[key]
+        same = sig8 == sig2
+        assert same.mean() >= 1.0 - 1e-4, (key, same.mean())
+        assert np.array_equal(rad8[same], rad2[same]), key
+        assert st8.camera_rays == st2.camera_rays and st8.error_flags == 0
+    img, rad, sig, st = out[(8, 0)]
+    assert st.shadow_rays > 0
+    ref = orc.render_nee(scene, w, h, spp, depth, seed=9, camera=scene.camera, want_samples=True)
+    _check_parity(img, rad, sig, ref, w, h, spp)
+    host.set_options(bvh_width=0, trace_block=0)
+
+
 def test_options_and_frames_are_validated(host):
     host.set_scene(q.make_scene("cornell36", host.lib))
     for bad in (dict(bvh_width=4), dict(refill_lanes=33), dict(trace_block=48), dict(max_depth=65)):
