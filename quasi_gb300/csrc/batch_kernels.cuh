@@ -153,7 +153,15 @@ __device__ __forceinline__ void trace_wide_refill_multi(Job& job, const BatchSce
             }
         }
         if (!__any_sync(0xffffffffu, active)) break;
-        if (active && wide_visit<ANY, STATS>(wide, tris, q, stack, err, cnt)) {
+        bool done = false;
+        if (active) {
+#pragma unroll 1
+            for (int i = 0; i < k_wide_visits_per_check; ++i) {
+                done = wide_visit<ANY, STATS>(wide, tris, q, stack, err, cnt);
+                if (done) break;
+            }
+        }
+        if (done) {
             TraceState st;
             st.r = q.r;
             st.tmax = q.tmax;

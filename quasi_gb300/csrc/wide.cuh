@@ -111,6 +111,12 @@ __device__ __forceinline__ int2* wide_stack_slot() {
     return s_wide_stack + (threadIdx.x >> 5) * (32 * wide_smem_stack<ANY>()) + (threadIdx.x & 31);
 }
 
+// Record visits a lane makes between two refill checks of its warp (ballot, fetch, vote).
+// Checking after every visit spends issue slots on the votes; after every second visit a
+// lane whose ray ended idles for at most one visit. 1080p frame of the 1M soup: 1 visit
+// 1420 Mrays/s, 2: 1444, 3: 1429, 4: 1437 (closest-hit 1 and any-hit 2: 1422).
+constexpr int k_wide_visits_per_check = 2;
+
 // Marks a finished traversal in WideRay::node (no record index is negative).
 constexpr int k_wide_done = static_cast<int>(0x80000000u);
 
@@ -179,7 +185,10 @@ __device__ __forceinline__ bool wide_leaf(const float4* __restrict__ tris, const
                                           TraceCounters& cnt) {
     const uint32_t x = static_cast<uint32_t>(~ref);
     const uint32_t pos = x >> 2;
-    const uint32_t count = ((x & 3u) + 1u) & 3u;
+    // With one-triangle leaves (k_wide_leaf_max = 1) a leaf that passed its box test holds
+    // exactly one triangle (empty slots never pass), and the loop is a single test: 1.8%
+    // faster on the 1M soup than decoding the count.
+    const uint32_t count = k_wide_leaf_max == 1 ? 1u : ((x & 3u) + 1u) & 3u;
     for (uint32_t j = 0; j < count; ++j) {
         if (STATS) ++cnt.tris;
         const float4* t = tris + 3ull * (pos + j);
@@ -448,7 +457,15 @@ __device__ __forceinline__ void trace_wide_refill(Job& job, const float4* __rest
             }
         }
         if (!__any_sync(0xffffffffu, active)) break;
-        if (active && wide_visit<ANY, STATS>(wide, tris, q, stack, err, cnt)) {
+        bool done = false;
+        if (active) {
+#pragma unroll 1
+            for (int i = 0; i < k_wide_visits_per_check; ++i) {
+                done = wide_visit<ANY, STATS>(wide, tris, q, stack, err, cnt);
+                if (done) break;
+            }
+        }
+        if (done) {
             TraceState s;
             s.r = q.r;
             s.tmax = q.tmax;
