@@ -38,8 +38,9 @@
 namespace quasi {
 
 // Triangles per leaf. Runs of 2-3 triangles save record visits, but the union box of a
-// Morton run is much larger than its triangles' boxes: on the 1M soup they doubled the
-// triangle tests per ray (8.3 vs 3.7 for camera rays), so every leaf holds one triangle.
+// Morton run is much larger than its triangles' boxes. On the 1M soup (1080p frame),
+// closest-hit visits / triangle tests per ray and Mrays/s: one triangle 24.0 / 5.3, 1442;
+// up to two 23.0 / 6.7, 1381; up to three 21.4 / 10.8, 1264. Every leaf holds one triangle.
 constexpr int k_wide_leaf_max = 1;
 constexpr int k_wide_stack = 96;      // (ref, t_near) entries per ray
 constexpr int k_wide_node_f4 = 6;     // float4 per wide record
