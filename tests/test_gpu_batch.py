@@ -13,19 +13,35 @@ pytestmark = pytest.mark.gpu
 
 DEPTH = 6
 # (spec, width, height, spp): uneven triangle counts, sizes that are not multiples of the
-# 8x4 pixel tile, and spp that splits across waves.
+# 8x4 pixel tile, and spp that splits across waves. "needles" is a scene of long thin
+# triangles whose rays stack past the shared-memory part of the traversal stacks.
 SCENES = [
     ("soup:n=1000,seed=1", 64, 64, 4),
     ("soup:n=20000,seed=2", 96, 54, 16),
     ("soup:n=3000,seed=3", 128, 128, 3),
     ("soup:n=150000,seed=4", 200, 120, 5),
     ("cornell36", 64, 64, 8),
+    ("needles", 48, 40, 4),
 ]
+
+
+def _needles(n=20000, seed=4, width=0.01) -> q.Scene:
+    """Long thin triangles across the unit cube: large overlapping boxes, rare hits."""
+    rng = np.random.default_rng(seed)
+    a = rng.random((n, 3)) * 0.9 + 0.05
+    b = rng.random((n, 3)) * 0.9 + 0.05
+    d = rng.normal(0.0, 1.0, (n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    v = np.concatenate([a, b, a + d * width], axis=1).astype(np.float32)
+    emission = np.zeros((n, 3), np.float32)
+    emission[::31] = (4.0, 3.5, 3.0)
+    cam = {"position": (0.5, 0.5, -1.0), "target": (0.5, 0.5, 0.5), "fov": 40.0}
+    return q.Scene(v, np.full((n, 3), 0.7, np.float32), emission, cam)
 
 
 @pytest.fixture(scope="module")
 def scenes(cuda_ok):
-    return [(q.make_scene(spec), w, h, spp) for spec, w, h, spp in SCENES]
+    return [(_needles() if spec == "needles" else q.make_scene(spec), w, h, spp) for spec, w, h, spp in SCENES]
 
 
 @pytest.fixture(scope="module")
