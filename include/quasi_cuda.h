@@ -423,10 +423,11 @@ Q_CUDA_EXPORT int Q_cuda_batch_set_materials_device(Q_cuda_batch* batch, const f
  * graph like the frame. */
 Q_CUDA_EXPORT int Q_cuda_batch_backward(Q_cuda_batch* batch, const float* device_grad_image,
                                         float* device_grad_albedo, float* device_grad_emission, void* stream);
-/* Times short frames (at most tune_spp = 1 sample per pixel of every scene) of each
- * candidate form, wave size, block size and fetch size, keeps the fastest in the options,
- * writes them to *chosen (may be NULL) and resets the accumulation. budget_ms bounds the
- * time spent (0 = 5000 ms). */
+/* Times frames of each candidate form, wave size, block size and fetch size (binary LBVH)
+ * or refill threshold (8-wide records), keeps the fastest in the options, writes them to
+ * *chosen (may be NULL) and resets the accumulation. The frames are the batch's own when
+ * the search over them fits half of budget_ms, else capped at fewer samples per pixel (at
+ * least 1). budget_ms bounds the time spent (0 = 5000 ms). */
 Q_CUDA_EXPORT int Q_cuda_batch_autotune(Q_cuda_batch* batch, double budget_ms, Q_cuda_batch_options* chosen);
 /* Message of the batch's last failed call (owned by the batch). */
 Q_CUDA_EXPORT const char* Q_cuda_batch_last_error(Q_cuda_batch* batch);

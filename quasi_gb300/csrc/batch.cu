@@ -663,14 +663,19 @@ int BatchRenderer::time_frame(float& ms) {
 }
 
 // Coordinate search over form, wave size, block size and fetch size (warp chunks over the
-// binary LBVH) or refill threshold (8-wide records) on 1-spp frames.
+// binary LBVH) or refill threshold (8-wide records). Candidates are timed on the batch's own
+// frame when the whole search over it fits half the budget, else on frames capped at fewer
+// samples per pixel (at least 1) so that it does. The cap matters: a 1-spp frame of 64 small
+// scenes weighs the wavefront form's fixed launch work 4x more than their 4-spp frame, where
+// the wavefront form is the faster one (3.1 vs 4.6 ms per frame on GB300), and a search on
+// 1-spp frames chose the megakernel.
 int BatchRenderer::autotune(double budget_ms, Q_cuda_batch_options* chosen) {
     if (budget_ms <= 0.0) budget_ms = 5000.0;
     const auto t0 = std::chrono::steady_clock::now();
     auto elapsed = [&]() {
         return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     };
-    constexpr uint32_t tune_spp = 1;
+    uint32_t tune_spp = 1;
     auto measure = [&](const Q_cuda_batch_options& o, float& ms) -> int {
         opt_ = o;
         int rc = plan(tune_spp);
@@ -681,6 +686,17 @@ int BatchRenderer::autotune(double budget_ms, Q_cuda_batch_options* chosen) {
     float best_ms = 0.f;
     int rc = measure(best, best_ms);
     if (rc) return rc;
+    // A frame capped at c samples per pixel costs at most c times the 1-spp frame, and each
+    // of the ~12 candidates times two frames.
+    constexpr double k_candidates = 12.0;
+    uint32_t max_spp = 1;
+    for (const HostScene& h : scenes_) max_spp = std::max(max_spp, h.spp);
+    const double cap = 0.5 * budget_ms / k_candidates / (2.0 * std::max(static_cast<double>(best_ms), 1e-3));
+    tune_spp = cap >= max_spp ? 0xffffffffu : std::max<uint32_t>(1, static_cast<uint32_t>(cap));
+    if (tune_spp != 1) {
+        rc = measure(best, best_ms);
+        if (rc) return rc;
+    }
     const uint32_t forms[] = {QUASI_BATCH_WAVEFRONT, QUASI_BATCH_MEGAKERNEL};
     const uint32_t waves[] = {8u << 20, 16u << 20, 32u << 20, 64u << 20};
     const uint32_t blocks[] = {64, 128, 256};
