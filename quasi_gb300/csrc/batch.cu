@@ -5,8 +5,9 @@
 // planes and packs them into waves of at most wave_paths path slots; the item table is
 // uploaded to the device, where it is the work queue every kernel of the frame reads. The
 // frame's launch sequence (all waves of all scenes) is captured once into a CUDA graph and
-// replayed by render(); the adjoint sequence likewise. autotune() times short frames of
-// candidate launch configurations and keeps the fastest.
+// replayed by render(); the adjoint sequence likewise. autotune() times frames of
+// candidate launch configurations (the batch's own, or capped at fewer samples per pixel
+// when those would not fit its budget) and keeps the fastest.
 #include "batch.hpp"
 #include "batch_kernels.cuh"
 
