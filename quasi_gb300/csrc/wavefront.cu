@@ -800,7 +800,7 @@ int Renderer::autotune(double budget_ms) {
                               : dim == 2 ? o.trace_block
                               : wide     ? o.refill_lanes
                                          : o.smem_levels;
-            if (field == v || (dim == 2 && field == 0 && v == 128)) continue;
+            if (field == v || (dim == 2 && field == 0 && v == (wide ? 256u : 128u))) continue;
             if (dim == 3 && wide && field == 0 && v == static_cast<uint32_t>(k_wide_refill_lanes)) continue;
             if (dim == 2 && o.megakernel) continue;  // the megakernel runs 128-thread blocks
             if (dim == 3 && o.megakernel) continue;
