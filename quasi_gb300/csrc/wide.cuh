@@ -72,9 +72,9 @@ template <bool ANY>
 __host__ __device__ constexpr int wide_smem_stack() {
     return ANY ? QUASI_WIDE_SMEM_STACK_ANY : QUASI_WIDE_SMEM_STACK;
 }
-static_assert(wide_smem_stack<false>() >= 0 && wide_smem_stack<false>() <= k_wide_stack &&
-                  wide_smem_stack<true>() >= 0 && wide_smem_stack<true>() <= k_wide_stack,
-              "shared stack entries");
+static_assert(wide_smem_stack<false>() >= 0 && wide_smem_stack<false>() < k_wide_stack &&
+                  wide_smem_stack<true>() >= 0 && wide_smem_stack<true>() < k_wide_stack,
+              "shared stack entries (the thread-local part keeps at least one)");
 static_assert(sizeof(int2) * wide_smem_stack<false>() * 256 <= 48 * 1024 &&
                   sizeof(int2) * wide_smem_stack<true>() * 256 <= 48 * 1024,
               "a 256-thread trace block stays within the default dynamic shared memory limit");
