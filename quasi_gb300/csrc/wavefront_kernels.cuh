@@ -112,8 +112,9 @@ __global__ void k_tally(const int* __restrict__ counters, uint32_t waves, uint32
 }
 
 // Minimum resident 256-thread blocks per SM asked of the compiler for k_shade (a register
-// cap). With 1 it takes 141 registers and the 1080p frame's shading costs 138 ms; 2 blocks
-// (128 registers) or 4 (64, with spills) cost 101 ms on GB300.
+// cap). Before the shading table it took 141 registers uncapped and the 1080p frame's
+// shading cost 138 ms; 2 blocks (128 registers) or 4 (64, with spills) cost 101 ms on
+// GB300. Now it takes 119 registers at 2 blocks (50 ms); 3 blocks (85 registers) cost 53 ms.
 #ifndef QUASI_SHADE_MIN_BLOCKS
 #define QUASI_SHADE_MIN_BLOCKS 2
 #endif
