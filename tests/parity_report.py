@@ -34,6 +34,31 @@ WORKLOADS = [
 ]
 
 
+def error_stats(g_img, g_rad, g_sig, o_mean, o_samp, o_sig, spp: int) -> dict:
+    """Statistics over n pixels: g_img (n, 3) GPU pixel means, g_rad (n, spp, 3) GPU samples,
+    g_sig (n, spp) GPU path signatures, and the oracle's o_mean, o_samp, o_sig alike."""
+    g_img = np.asarray(g_img, np.float64).reshape(-1, 3)
+    g_rad = np.asarray(g_rad, np.float64).reshape(-1, spp, 3)
+    o_mean = np.asarray(o_mean, np.float64).reshape(-1, 3)
+    o_samp = np.asarray(o_samp, np.float64).reshape(-1, spp, 3)
+    match = np.asarray(g_sig).reshape(-1, spp) == np.asarray(o_sig).reshape(-1, spp)
+    px_ok = match.all(-1)
+    p_err = (np.abs(g_img - o_mean) / np.maximum(np.abs(o_mean), FLOOR)).max(-1)
+    s_err = (np.abs(g_rad - o_samp) / np.maximum(np.abs(o_samp), FLOOR)).max(-1)
+    ok = p_err[px_ok]
+    return {
+        "pixels": int(px_ok.size),
+        "samples": int(match.size),
+        "max_rel_err": float(ok.max()) if ok.size else 0.0,
+        "p99.99_rel_err": float(np.quantile(ok, 0.9999)) if ok.size else 0.0,
+        "max_sample_rel_err": float(s_err[match].max()) if match.any() else 0.0,
+        "pixels_over_1e-4_non_divergent": int((ok > TOL).sum()),
+        "pixels_over_1e-4_divergent": int((p_err[~px_ok] > TOL).sum()),
+        "divergent_pixels": int((~px_ok).sum()),
+        "divergent_samples": int((~match).sum()),
+    }
+
+
 def report(name, spec, w, h, spp, depth, seed, n_pix) -> dict:
     host = q.PluginHost(width=w, height=h)
     scene = q.make_scene(spec, host.lib)
@@ -51,28 +76,10 @@ def report(name, spec, w, h, spp, depth, seed, n_pix) -> dict:
         pix = np.random.default_rng(5).choice(w * h, size=n_pix, replace=False).astype(np.uint32)
         ref = orc.render_nee(scene, w, h, spp, depth, seed=seed, pixels=pix, want_samples=True)
     ys, xs = pix // w, pix % w
-    g_img = img[ys, xs, :3].astype(np.float64)
-    g_rad = rad[ys, xs].astype(np.float64)
-    o_mean = ref["mean"].reshape(-1, 3)
-    o_samp = ref["samples"].reshape(-1, spp, 3)
-    match = sig[ys, xs].reshape(-1, spp) == ref["sig"].reshape(-1, spp)
-    px_ok = match.all(-1)
-    p_err = (np.abs(g_img - o_mean) / np.maximum(np.abs(o_mean), FLOOR)).max(-1)
-    s_err = (np.abs(g_rad - o_samp) / np.maximum(np.abs(o_samp), FLOOR)).max(-1)
-    ok = p_err[px_ok]
-    return {
-        "workload": name,
-        "pixels": int(pix.size),
-        "samples": int(match.size),
-        "max_rel_err": float(ok.max()) if ok.size else 0.0,
-        "p99.99_rel_err": float(np.quantile(ok, 0.9999)) if ok.size else 0.0,
-        "max_sample_rel_err": float(s_err[match].max()) if match.any() else 0.0,
-        "pixels_over_1e-4_non_divergent": int((ok > TOL).sum()),
-        "pixels_over_1e-4_divergent": int((p_err[~px_ok] > TOL).sum()),
-        "divergent_pixels": int((~px_ok).sum()),
-        "divergent_samples": int((~match).sum()),
-        "error_flags": int(st.error_flags),
-    }
+    out = {"workload": name}
+    out.update(error_stats(img[ys, xs, :3], rad[ys, xs], sig[ys, xs], ref["mean"], ref["samples"], ref["sig"], spp))
+    out["error_flags"] = int(st.error_flags)
+    return out
 
 
 def main() -> None:
