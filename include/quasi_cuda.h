@@ -297,7 +297,9 @@ Q_CUDA_EXPORT int Q_cuda_radix_sort_pairs(uint32_t* device_keys, uint32_t* devic
  * Limits and behaviour:
  *  - n above QUASI_NOALLOC_SORT_MAX_KEYS returns QUASI_ERR_TOO_LARGE and touches nothing;
  *  - the first call on a device looks up the array's device address (cudaGetSymbolAddress,
- *    with that device current); make that first call before any stream capture;
+ *    with that device current) and keeps it for the life of the process; make that first
+ *    call before any stream capture, and do not reset the device's primary context
+ *    (cudaDeviceReset) after it: the module would be reloaded and the kept address stale;
  *  - all calls share the one array and it keeps the last call's contents, so calls that
  *    overlap on the GPU (other streams, other threads) race; serialise them on one stream;
  *  - the sort is enqueued on `stream` and the function returns without waiting for it. */

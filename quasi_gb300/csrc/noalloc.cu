@@ -34,7 +34,9 @@ uint32_t* g_scratch_addr[k_max_devices] = {};
 
 // Device address of g_sort_scratch on the current device. In host code the name
 // g_sort_scratch is only a host-side stand-in, so the address is looked up once per device
-// (with that device current) and cached.
+// (with that device current) and cached for the life of the process. A cudaDeviceReset of
+// that device after the first call would reload the module and leave the cached address
+// stale, which is why callers must not reset the primary context after it.
 cudaError_t scratch_for_current_device(uint32_t** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);

@@ -39,9 +39,12 @@ def _sort(lib, fn_name: str, keys: np.ndarray, vals: np.ndarray, bits: int):
 def test_noalloc_sort_matches_allocating_sort_on_two_calls_in_a_row(cuda_ok):
     lib = q.load_library()
     rng = np.random.default_rng(2024)
-    # Call 1 fills the whole scratch; call 2 is smaller and uses fewer passes, so anything
-    # it wrongly read back from call 1's leftovers would show up as a mismatch.
-    cases = [(MAX_KEYS, 32), (300_001, 30)]
+    # Call 1 fills the whole scratch (32 bits: 4 passes of 8 bits, so the result ends in the
+    # caller's buffer). Calls 2 and 3 are smaller and take an odd number of passes (24 bits:
+    # 3, 8 bits: 1), so their result ends in the static scratch and is copied back to the
+    # caller's buffer; anything read back from an earlier call's leftovers would show up as
+    # a mismatch.
+    cases = [(MAX_KEYS, 32), (300_001, 24), (5_003, 8)]
     for n, bits in cases:
         keys = rng.integers(0, 1 << bits, size=n, dtype=np.uint64).astype(np.uint32)
         keys[: n // 4] = keys[7]  # duplicates: the sort must stay stable
