@@ -501,7 +501,8 @@ def run_ours(args) -> None:
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": WORKLOAD, "tri_count": scene.tri_count, "width": WIDTH, "height": HEIGHT,
                            "spp": SPP, "max_depth": DEPTH, "rays_per_step": rays / args.steps / world,
-                           "bvh_ms": st.bvh_ms, "l2": "flushed before every step (256 MiB write, inside the "
+                           "bvh_ms": st.bvh_ms, "redecided_rays_per_step": st.redecided_rays,
+                           "l2": "flushed before every step (256 MiB write, inside the "
                            "timed region)", "parallelism": f"replicas x{world}", "wave_spp": args.wave_spp,
                            "trace_block": args.trace_block, "refill_lanes": args.refill_lanes,
                            "bvh": "binary LBVH" if args.bvh_width == 2 else "8-wide records collapsed from the LBVH"},

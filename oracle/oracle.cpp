@@ -273,8 +273,8 @@ inline float half_area_o(const float lo[3], const float hi[3]) {
 
 // 8-wide record of every internal node of b, 24 words each, restating k_collapse8
 // (quasi_gb300/csrc/bvh.cu): greedy opening of the largest child by surface area, leaves of
-// one triangle, child boxes on an 8-bit power-of-two grid rounded
-// outwards, children placed in slots by direction (Ylitie, Karras and Laine 2017).
+// one triangle, child boxes padded by the scene's Delta and put on an 8-bit power-of-two grid
+// rounded outwards, children placed in slots by direction (Ylitie, Karras and Laine 2017).
 void collapse8(const Lbvh& b, std::vector<uint32_t>& out) {
     const uint32_t nodes = b.n > 1 ? b.n - 1 : (b.n == 1 ? 1 : 0);
     out.assign(24ull * nodes, 0u);
@@ -293,6 +293,11 @@ void collapse8(const Lbvh& b, std::vector<uint32_t>& out) {
             e.size = b.range[2ull * e.ref + 1] - e.first + 1;
         }
     };
+    // Delta = 2^-16 S, S the largest absolute coordinate of the root's child boxes (every
+    // vertex): the spatial box padding of the FP32 traversal (CUDA scene_box_pad)
+    float smax = 0.0f;
+    for (size_t k = 0; k < std::min<size_t>(12, b.box.size()); ++k) smax = std::max(smax, std::fabs(b.box[k]));
+    const float pad = std::ldexp(std::max(smax, std::ldexp(1.0f, -100)), -16);
     for (uint32_t nb = 0; nb < nodes; ++nb) {
         WideEntryO e[8];
         entry(static_cast<int>(nb), 0, e[0]);
@@ -324,10 +329,14 @@ void collapse8(const Lbvh& b, std::vector<uint32_t>& out) {
                 hi[a] = std::fmax(hi[a], e[i].hi[a]);
             }
         }
+        // grid over the node box padded by the scene's Delta (padded child boxes, lower planes
+        // rounded down, upper planes up)
+        float glo[3];
         uint32_t ex[3];
         double inv_s[3];
         for (int a = 0; a < 3; ++a) {
-            const float x = div255_up(sub_round(hi[a], lo[a], true));
+            glo[a] = sub_round(lo[a], pad, false);
+            const float x = div255_up(sub_round(sub_round(hi[a], -pad, true), glo[a], true));
             uint32_t bits;
             std::memcpy(&bits, &x, 4);
             const int eb = static_cast<int>((bits >> 23) & 0xffu);
@@ -375,8 +384,10 @@ void collapse8(const Lbvh& b, std::vector<uint32_t>& out) {
         for (int i = 0; i < count; ++i) {
             const int s = slot_of[i];
             for (int a = 0; a < 3; ++a) {
-                const double ql = std::floor(double(sub_round(e[i].lo[a], lo[a], false)) * inv_s[a]);
-                const double qh = std::ceil(double(sub_round(e[i].hi[a], lo[a], true)) * inv_s[a]);
+                const double ql =
+                    std::floor(double(sub_round(sub_round(e[i].lo[a], pad, false), glo[a], false)) * inv_s[a]);
+                const double qh =
+                    std::ceil(double(sub_round(sub_round(e[i].hi[a], -pad, true), glo[a], true)) * inv_s[a]);
                 const uint32_t bl = static_cast<uint32_t>(std::min(std::max(ql, 0.0), 255.0));
                 const uint32_t bh = static_cast<uint32_t>(std::min(std::max(qh, 0.0), 255.0));
                 qlo[a][s >> 2] = (qlo[a][s >> 2] & ~(255u << (8 * (s & 3)))) | (bl << (8 * (s & 3)));
@@ -389,9 +400,9 @@ void collapse8(const Lbvh& b, std::vector<uint32_t>& out) {
                 refs[s] = ~((e[i].first << 2) | (e[i].size - 1));
             }
         }
-        std::memcpy(&w[0], &lo[0], 4);
-        std::memcpy(&w[1], &lo[1], 4);
-        std::memcpy(&w[2], &lo[2], 4);
+        std::memcpy(&w[0], &glo[0], 4);
+        std::memcpy(&w[1], &glo[1], 4);
+        std::memcpy(&w[2], &glo[2], 4);
         w[3] = ex[0] | (ex[1] << 8) | (ex[2] << 16) | (imask << 24);
         for (int a = 0; a < 3; ++a) {
             w[4 + 4 * a] = qlo[a][0];

@@ -101,7 +101,7 @@ class Q_cuda_stats(C.Structure):
                 ("node_visits", C.c_uint64), ("tri_tests", C.c_uint64), ("shadow_node_visits", C.c_uint64),
                 ("shadow_tri_tests", C.c_uint64), ("total_rays", C.c_uint64), ("samples_accumulated", C.c_uint64),
                 ("kernel_launches", C.c_uint32), ("error_flags", C.c_uint32), ("frame_ms", C.c_double),
-                ("bvh_ms", C.c_double), ("adjoint_rays", C.c_uint64)]
+                ("bvh_ms", C.c_double), ("adjoint_rays", C.c_uint64), ("redecided_rays", C.c_uint64)]
 
     @property
     def rays(self) -> int:
@@ -129,7 +129,7 @@ class Q_cuda_batch_stats(C.Structure):
                 ("shadow_rays", C.c_uint64), ("node_visits", C.c_uint64), ("tri_tests", C.c_uint64),
                 ("scenes", C.c_uint32), ("waves", C.c_uint32), ("kernels_per_frame", C.c_uint32),
                 ("error_flags", C.c_uint32), ("tri_total", C.c_uint64), ("px_total", C.c_uint64),
-                ("frame_ms", C.c_double), ("adjoint_rays", C.c_uint64)]
+                ("frame_ms", C.c_double), ("adjoint_rays", C.c_uint64), ("redecided_rays", C.c_uint64)]
 
     @property
     def rays(self) -> int:

@@ -41,7 +41,7 @@ BatchRenderer::~BatchRenderer() {
     drop_graphs();
     for (auto& b : bvh_) b->release();
     for (DeviceBuffer* b : {&tri_in_, &albedo_, &emission_, &emitters_, &accum_, &comp_, &aov_a_, &aov_n_, &table_,
-                            &items_, &queue_[0], &queue_[1], &hits_, &shadow_, &beta_, &lpath_, &pa_, &pn_, &ray_ff_,
+                            &items_, &queue_[0], &queue_[1], &hits_, &shadow_, &beta_, &lpath_, &pa_, &pn_, &ray_ff_, &shadow_ff_, &defer_,
                             &meta_, &counters_, &adj_counters_, &stats_dev_, &err_dev_, &grad_image_, &grad_albedo_,
                             &grad_emission_})
         b->release();
@@ -147,12 +147,12 @@ int BatchRenderer::create(const Q_cuda_batch_scene* scenes, uint32_t count, cons
             B_TRY(cudaMemcpy(emitters_.ptr, em.data(), sizeof(int) * em.size(), cudaMemcpyHostToDevice), "h2d");
     }
     for (DeviceBuffer* b : {&accum_, &comp_, &aov_a_, &aov_n_}) B_TRY(b->reserve(sizeof(float4) * px), "image pool");
-    B_TRY(stats_dev_.reserve(sizeof(unsigned long long) * 8), "stats");
+    B_TRY(stats_dev_.reserve(sizeof(unsigned long long) * 9), "stats");
     B_TRY(err_dev_.reserve(sizeof(uint32_t)), "err");
     B_TRY(cudaMemsetAsync(err_dev_.ptr, 0, sizeof(uint32_t), s), "memset");
-    B_TRY(cudaMallocHost(&stats_host_, sizeof(unsigned long long) * 8), "pinned");
+    B_TRY(cudaMallocHost(&stats_host_, sizeof(unsigned long long) * 9), "pinned");
     B_TRY(cudaMallocHost(&err_host_, sizeof(uint32_t)), "pinned");
-    std::memset(stats_host_, 0, sizeof(unsigned long long) * 8);
+    std::memset(stats_host_, 0, sizeof(unsigned long long) * 9);
     *err_host_ = 0;
     B_TRY(cudaEventCreate(&ev0_), "event");
     B_TRY(cudaEventCreate(&ev1_), "event");
@@ -223,8 +223,9 @@ int BatchRenderer::upload_table() {
 // packs them into waves of at most W path slots, scene after scene.
 int BatchRenderer::plan(uint32_t spp_cap) {
     // per path slot: two ray queues (2 x 32), hit 16, shadow ray 48, beta, radiance and two
-    // AOVs (4 x 16), double-float ray 48, (scene, local path) 8
-    constexpr size_t bytes_per_path = 248;
+    // AOVs (4 x 16), double-float ray 48, (scene, local path) 8, exact shadow segment 48,
+    // fixup list entry 4
+    constexpr size_t bytes_per_path = 300;
     uint32_t W = opt_.wave_paths ? opt_.wave_paths
                                  : static_cast<uint32_t>(wave_paths_fitting(k_default_wave_paths, bytes_per_path,
                                                                             size_t(wave_capacity_) * bytes_per_path));
@@ -279,12 +280,14 @@ int BatchRenderer::ensure_buffers() {
         B_TRY(pa_.reserve(sizeof(float4) * paths), "aov");
         B_TRY(pn_.reserve(sizeof(float4) * paths), "aov");
         B_TRY(ray_ff_.reserve(sizeof(float4) * 3ull * paths), "ray_ff");
+        B_TRY(shadow_ff_.reserve(sizeof(float4) * 3ull * paths), "shadow_ff");
+        B_TRY(defer_.reserve(sizeof(int) * paths), "defer");
         B_TRY(meta_.reserve(sizeof(uint2) * paths), "meta");
         wave_capacity_ = paths;
         graphs_dirty_ = true;
     }
     const size_t nw = std::max<size_t>(waves_.size(), 1);
-    const size_t need = sizeof(int) * 4ull * opt_.max_depth * nw;
+    const size_t need = sizeof(int) * k_batch_counters_per_bounce * opt_.max_depth * nw;
     if (need > counters_.bytes || sizeof(int) * nw > adj_counters_.bytes) graphs_dirty_ = true;
     B_TRY(counters_.reserve(need), "counters");
     B_TRY(adj_counters_.reserve(sizeof(int) * nw), "counters");
@@ -323,7 +326,7 @@ int BatchRenderer::record_frame(cudaStream_t s, uint32_t& launches) {
     const BatchSceneDev* table = table_.as<BatchSceneDev>();
     const BatchItem* items = items_.as<BatchItem>();
     PathDev pd{beta_.as<float4>(), lpath_.as<float4>(), pa_.as<float4>(), pn_.as<float4>(), ray_ff_.as<float4>(),
-               nullptr};
+               nullptr, shadow_ff_.as<float4>()};
     uint2* meta = meta_.as<uint2>();
     uint32_t* err = err_dev_.as<uint32_t>();
     unsigned long long* st = stats_dev_.as<unsigned long long>();
@@ -332,7 +335,7 @@ int BatchRenderer::record_frame(cudaStream_t s, uint32_t& launches) {
     const int mb = std::min(tb, 128);
     const int chunk = static_cast<int>(opt_.fetch_rays);
     const int refill = static_cast<int>(opt_.refill_lanes);
-    const size_t per_wave = 4ull * D;
+    const size_t per_wave = size_t(k_batch_counters_per_bounce) * D;
     B_TRY(cudaMemsetAsync(counters_.ptr, 0, sizeof(int) * per_wave * std::max<size_t>(waves_.size(), 1), s), "memset");
     const bool stats = opt_.collect_stats != 0;
     const bool wide = opt_.bvh_width != 2;
@@ -343,6 +346,9 @@ int BatchRenderer::record_frame(cudaStream_t s, uint32_t& launches) {
     auto km = stats ? k_batch_megakernel<true> : k_batch_megakernel<false>;
     const int grid_c = grid_c_, grid_s = grid_s_, grid_m = grid_m_;
     const int grid_shade = sm * 8;
+    const int grid_fixup = grid_c;
+    auto kfc = wide ? k_batch_fixup<ClosestJob, true> : k_batch_fixup<ClosestJob, false>;
+    auto kfs = wide ? k_batch_fixup<ShadowJob, true> : k_batch_fixup<ShadowJob, false>;
     const int cap = static_cast<int>(wave_capacity_);
     for (size_t w = 0; w < waves_.size(); ++w) {
         const Wave& wv = waves_[w];
@@ -366,19 +372,28 @@ int BatchRenderer::record_frame(cudaStream_t s, uint32_t& launches) {
                 int* c_shadow = cnt + D + (k - 1);
                 int* f_cur = cnt + 2 * D + (k - 1);
                 int* f_shadow = cnt + 3 * D + (k - 1);
+                const ClosestJob cjob{qcur, hits_.as<float4>(), ray_ff_.as<float4>(),
+                                      DeferList{defer_.as<int>(), cnt + 4 * D + (k - 1)}};
+                const ShadowJob sjob{shadow_.as<float4>(), pd, DeferList{defer_.as<int>(), cnt + 5 * D + (k - 1)}};
                 B_TRY(QUASI_LAUNCH(prof_, "batch_trace_closest", s,
-                                   (kc<<<grid_c, tb, smem_c_, s>>>(table, meta, qcur, hits_.as<float4>(), c_cur, cap, chunk,
-                                                             refill, f_cur, err, st))),
+                                   (kc<<<grid_c, tb, smem_c_, s>>>(table, meta, cjob, c_cur, cap, chunk, refill, f_cur, err,
+                                                                   st))),
                       "batch_trace_closest");
+                B_TRY(QUASI_LAUNCH(prof_, "batch_fixup_closest", s,
+                                   (kfc<<<grid_fixup, tb, smem_c_, s>>>(table, meta, cjob, cnt + 6 * D + (k - 1), err))),
+                      "batch_fixup_closest");
                 B_TRY(QUASI_LAUNCH(prof_, "batch_shade", s,
                                    (k_batch_shade<<<grid_shade, 256, 0, s>>>(table, meta, pd, k, qcur, hits_.as<float4>(),
                                                                              c_cur, cap, qnext, k < D ? c_next : nullptr,
                                                                              shadow_.as<float4>(), c_shadow))),
                       "batch_shade");
                 B_TRY(QUASI_LAUNCH(prof_, "batch_trace_shadow", s,
-                                   (ks<<<grid_s, tb, smem_s_, s>>>(table, meta, pd, shadow_.as<float4>(), c_shadow, cap, chunk,
-                                                             refill, f_shadow, err, st))),
+                                   (ks<<<grid_s, tb, smem_s_, s>>>(table, meta, sjob, c_shadow, cap, chunk, refill, f_shadow,
+                                                                   err, st))),
                       "batch_trace_shadow");
+                B_TRY(QUASI_LAUNCH(prof_, "batch_fixup_shadow", s,
+                                   (kfs<<<grid_s, tb, smem_s_, s>>>(table, meta, sjob, cnt + 7 * D + (k - 1), err))),
+                      "batch_fixup_shadow");
             }
         }
         B_TRY(QUASI_LAUNCH(prof_, "batch_accumulate", s,
@@ -465,7 +480,7 @@ int BatchRenderer::ensure_graphs() {
         // Plain launches: count the kernels of one frame without enqueueing them.
         const uint32_t D = opt_.max_depth;
         const uint32_t nw = static_cast<uint32_t>(waves_.size());
-        launches = opt_.form == QUASI_BATCH_MEGAKERNEL ? 2 * nw + 1 : nw * (2 + 3 * D) + 2;
+        launches = opt_.form == QUASI_BATCH_MEGAKERNEL ? 2 * nw + 1 : nw * (2 + 5 * D) + 2;
     }
     kernels_per_frame_ = launches;
     graphs_dirty_ = false;
@@ -500,7 +515,7 @@ int BatchRenderer::reset() {
     cudaStream_t s = stream_;
     for (DeviceBuffer* b : {&accum_, &comp_, &aov_a_, &aov_n_})
         if (b->ptr) B_TRY(cudaMemsetAsync(b->ptr, 0, b->bytes, s), "memset");
-    B_TRY(cudaMemsetAsync(stats_dev_.ptr, 0, sizeof(unsigned long long) * 8, s), "memset");
+    B_TRY(cudaMemsetAsync(stats_dev_.ptr, 0, sizeof(unsigned long long) * 9, s), "memset");
     B_TRY(QUASI_LAUNCH(prof_, "batch_rewind", s,
                        (k_batch_rewind<<<1, 256, 0, s>>>(table_.as<BatchSceneDev>(),
                                                          static_cast<uint32_t>(scenes_.size())))),
@@ -534,7 +549,7 @@ int BatchRenderer::synchronize() {
 int BatchRenderer::stats(Q_cuda_batch_stats* out) {
     if (!out) return fail(QUASI_ERR_INVALID, "null stats");
     B_TRY(cudaStreamSynchronize(stream_), "synchronize");
-    B_TRY(cudaMemcpy(stats_host_, stats_dev_.ptr, sizeof(unsigned long long) * 8, cudaMemcpyDeviceToHost), "d2h");
+    B_TRY(cudaMemcpy(stats_host_, stats_dev_.ptr, sizeof(unsigned long long) * 9, cudaMemcpyDeviceToHost), "d2h");
     B_TRY(cudaMemcpy(err_host_, err_dev_.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost), "d2h");
     Q_cuda_batch_stats r{};
     r.frames = stats_host_[4];
@@ -544,6 +559,7 @@ int BatchRenderer::stats(Q_cuda_batch_stats* out) {
     r.node_visits = stats_host_[0] + stats_host_[2];
     r.tri_tests = stats_host_[1] + stats_host_[3];
     r.adjoint_rays = stats_host_[7];
+    r.redecided_rays = stats_host_[8];
     r.scenes = static_cast<uint32_t>(scenes_.size());
     r.waves = static_cast<uint32_t>(waves_.size());
     r.kernels_per_frame = kernels_per_frame_;

@@ -26,6 +26,8 @@
 
 #include "path.cuh"
 
+#include <type_traits>
+
 namespace quasi {
 
 struct BatchSceneDev {
@@ -102,12 +104,11 @@ __device__ __forceinline__ void trace_batches_multi(Job& job, const BatchSceneDe
                 float tmax;
                 int exclude;
                 job.load(i, o, d, tmax, exclude);
-                TraceState st;
-                st.r = make_ray(o, d);
-                st.tmax = tmax;
-                st.best = trace_bvh<ANY, STATS>(s.nodes, s.tris, s.n_tris, st.r, tmax, exclude, st.best_t, st.bu, st.bv,
-                                                err, cnt);
-                job.store(i, st);
+                const RayInv r = make_ray(o, d, s.n_tris ? scene_box_pad(s.nodes) : 0.0f);
+                TraceResult res;
+                res.prim = trace_bvh<ANY, STATS>(s.nodes, s.tris, nullptr, s.n_tris, r, tmax, exclude, res.t, res.u,
+                                                 res.v, err, cnt);
+                finish_ray(job, i, res);
             }
         }
     }
@@ -117,7 +118,9 @@ __device__ __forceinline__ void trace_batches_multi(Job& job, const BatchSceneDe
 // records: once `refill` lanes of a warp are idle they take the next rays with one atomic;
 // each lane traverses the records of its own ray's scene. Blocks are launched with
 // wide_stack_smem_bytes<ANY>(blockDim.x) of dynamic shared memory (the stacks' shared part).
-template <bool ANY, bool STATS, class Job>
+// ROBUST (the fixup kernel): undecided candidates are re-decided inline from job.exact(i)
+// and the scene's original-order vertices, and every ray is stored.
+template <bool ANY, bool STATS, class Job, bool ROBUST = false>
 __device__ __forceinline__ void trace_wide_refill_multi(Job& job, const BatchSceneDev* __restrict__ scenes,
                                                         const uint2* __restrict__ meta, int n, int refill,
                                                         int* __restrict__ fetch, uint32_t& err, TraceCounters& cnt) {
@@ -127,6 +130,9 @@ __device__ __forceinline__ void trace_wide_refill_multi(Job& job, const BatchSce
     stack.slot = wide_stack_slot<ANY>();
     const float4* wide = nullptr;
     const float4* tris = nullptr;
+    const float4* tri_in = nullptr;
+    using X = typename std::conditional<ROBUST, ExactPtr, ExactNone>::type;
+    X xr{};
     bool active = false, exhausted = false;
     int idx = 0;
     while (true) {
@@ -143,10 +149,12 @@ __device__ __forceinline__ void trace_wide_refill_multi(Job& job, const BatchSce
                     const SceneDev& s = scenes[meta[job.pid(idx)].x].s;
                     wide = s.wide;
                     tris = s.tris;
+                    tri_in = s.tri_in;
                     float3 o, d;
                     float tmax;
                     int exclude;
                     job.load(idx, o, d, tmax, exclude);
+                    if constexpr (ROBUST) xr = job.exact(idx);
                     wide_begin(q, o, d, tmax, exclude, s.n_tris);
                     active = true;
                 }
@@ -157,19 +165,16 @@ __device__ __forceinline__ void trace_wide_refill_multi(Job& job, const BatchSce
         if (active) {
 #pragma unroll 1
             for (int i = 0; i < k_wide_visits_per_check; ++i) {
-                done = wide_visit<ANY, STATS>(wide, tris, q, stack, err, cnt);
+                done = wide_visit<ANY, STATS, WideStack<wide_smem_stack<ANY>()>, ROBUST>(wide, tris, q, stack, err, cnt,
+                                                                                       tri_in, xr);
                 if (done) break;
             }
         }
         if (done) {
-            TraceState st;
-            st.r = q.r;
-            st.tmax = q.tmax;
-            st.best_t = q.best_t;
-            st.best = q.best;
-            st.bu = q.bu;
-            st.bv = q.bv;
-            job.store(idx, st);
+            if constexpr (ROBUST)
+                job.store(idx, trace_result(q.b));
+            else
+                finish_ray(job, idx, trace_result(q.b));
             active = false;
         }
     }
@@ -179,15 +184,14 @@ __device__ __forceinline__ void trace_wide_refill_multi(Job& job, const BatchSce
 // otherwise warp chunks over the scenes' binary LBVHs.
 template <bool STATS, bool WIDE>
 __global__ void __launch_bounds__(256, WIDE ? QUASI_WIDE_MIN_BLOCKS : 1) k_batch_trace_closest(const BatchSceneDev* __restrict__ scenes,
-                                                             const uint2* __restrict__ meta, const float4* __restrict__ q,
-                                                             float4* __restrict__ hits, const int* __restrict__ count,
+                                                             const uint2* __restrict__ meta, ClosestJob job,
+                                                             const int* __restrict__ count,
                                                              int capacity, int chunk, int refill, int* __restrict__ fetch,
                                                              uint32_t* __restrict__ err,
                                                              unsigned long long* __restrict__ stats) {
     const int n = min(*count, capacity);
     uint32_t e = 0;
     TraceCounters c;
-    ClosestJob job{q, hits};
     if (WIDE)
         trace_wide_refill_multi<false, STATS>(job, scenes, meta, n, refill, fetch, e, c);
     else
@@ -198,21 +202,61 @@ __global__ void __launch_bounds__(256, WIDE ? QUASI_WIDE_MIN_BLOCKS : 1) k_batch
 
 template <bool STATS, bool WIDE>
 __global__ void __launch_bounds__(256, WIDE ? QUASI_WIDE_MIN_BLOCKS : 1) k_batch_trace_shadow(const BatchSceneDev* __restrict__ scenes,
-                                                            const uint2* __restrict__ meta, PathDev p,
-                                                            const float4* __restrict__ sq, const int* __restrict__ count,
+                                                            const uint2* __restrict__ meta, ShadowJob job,
+                                                            const int* __restrict__ count,
                                                             int capacity, int chunk, int refill,
                                                             int* __restrict__ fetch, uint32_t* __restrict__ err,
                                                             unsigned long long* __restrict__ stats) {
     const int n = min(*count, capacity);
     uint32_t e = 0;
     TraceCounters c;
-    ShadowJob job{sq, p};
     if (WIDE)
         trace_wide_refill_multi<true, STATS>(job, scenes, meta, n, refill, fetch, e, c);
     else
         trace_batches_multi<true, STATS>(job, scenes, meta, n, chunk, fetch, e, c);
     if (e) atomicOr(err, e);
     flush_counters<STATS>(c, stats + 2);
+}
+
+// Re-traces the rays a batch trace kernel deferred (robust.cuh) with exact re-decisions: over
+// the 8-wide records of each ray's scene with per-lane refill (WIDE, launched like the wide
+// trace kernels), else over the binary LBVHs, one ray per thread.
+template <class Job, bool WIDE>
+__global__ void __launch_bounds__(256, WIDE ? QUASI_WIDE_MIN_BLOCKS : 1) k_batch_fixup(
+    const BatchSceneDev* __restrict__ scenes, const uint2* __restrict__ meta, Job job, int* __restrict__ fetch,
+    uint32_t* __restrict__ err) {
+    constexpr bool any = std::is_same<Job, ShadowJob>::value;
+    const int n = *job.deferred.count;
+    uint32_t e = 0;
+    TraceCounters cnt;
+    if constexpr (WIDE) {
+        FixupJob<Job> fj{job, job.deferred.list};
+        trace_wide_refill_multi<any, false, FixupJob<Job>, true>(fj, scenes, meta, n, k_wide_refill_lanes, fetch, e,
+                                                                 cnt);
+    } else {
+        const int lane = threadIdx.x & 31;
+        while (true) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(fetch, 32);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= n) break;
+            const int k = base + lane;
+            if (k < n) {
+                const int i = job.deferred.list[k];
+                const SceneDev& s = scenes[meta[job.pid(i)].x].s;
+                float3 o, d;
+                float tmax;
+                int exclude;
+                job.load(i, o, d, tmax, exclude);
+                const RayInv r = make_ray(o, d, s.n_tris ? scene_box_pad(s.nodes) : 0.0f);
+                TraceResult res;
+                res.prim = trace_bvh<any, false, false, true>(s.nodes, s.tris, s.tri_in, s.n_tris, r, tmax, exclude,
+                                                              res.t, res.u, res.v, e, cnt, job.exact(i));
+                job.store(i, res);
+            }
+        }
+    }
+    if (e) atomicOr(err, e);
 }
 
 __global__ void __launch_bounds__(256) k_batch_shade(const BatchSceneDev* __restrict__ scenes,
@@ -294,8 +338,9 @@ __global__ void __launch_bounds__(128) k_batch_megakernel(const BatchSceneDev* _
             if (x >= b.f.width || y >= b.f.height) continue;
             int nv = 0;
             float4 aa = make_float4(0.f, 0.f, 0.f, 0.f), an = aa;
+            const float pad = b.s.n_tris ? scene_box_pad(b.s.nodes) : 0.0f;
             const float3 L = trace_path<STATS>(b.f, b.s, x, y, b.f.sample_base + j, nullptr, nv, &aa, &an, nullptr, e,
-                                               c, rays, shadow_rays);
+                                               c, rays, shadow_rays, pad);
             p.lpath[gid] = make_float4(L.x, L.y, L.z, 0.f);
             p.aov_a[gid] = aa;
             p.aov_n[gid] = an;
@@ -350,32 +395,43 @@ __global__ void __launch_bounds__(128) k_batch_adjoint(const BatchSceneDev* __re
             const float3 d = mk3(grad_image[3 * px] * inv_spp, grad_image[3 * px + 1] * inv_spp,
                                  grad_image[3 * px + 2] * inv_spp);
             if (d.x == 0.0f && d.y == 0.0f && d.z == 0.0f) continue;
+            const float pad = b.s.n_tris ? scene_box_pad(b.s.nodes) : 0.0f;
             adjoint_path(b.f, b.s, x, y, b.f.sample_base - b.spp + j, d, grad_albedo + 3ull * b.tri_offset,
-                         grad_emission + 3ull * b.tri_offset, e, c, rays);
+                         grad_emission + 3ull * b.tri_offset, e, c, rays, pad);
         }
     }
     if (e) atomicOr(err, e);
     warp_add_count(rays, &stats[7]);
 }
 
-// Adds the frame's closest-hit and shadow queue lengths to stats[5] and stats[6]. One warp.
+// Per-wave counters of the wavefront form, k_batch_counters_per_bounce per bounce: queue
+// lengths [0, 2D), trace fetch counters [2D, 4D), deferred rays [4D, 6D), fixup fetch
+// counters [6D, 8D).
+constexpr uint32_t k_batch_counters_per_bounce = 8;
+
+// Adds the frame's closest-hit and shadow queue lengths to stats[5] and stats[6] and the
+// rays re-traced by the fixup kernels to stats[8]. One warp.
 __global__ void k_batch_tally(const int* __restrict__ counters, uint32_t waves, uint32_t depth,
                               unsigned long long* __restrict__ stats) {
-    unsigned long long closest = 0, shadow = 0;
+    unsigned long long closest = 0, shadow = 0, redecided = 0;
     for (uint32_t i = threadIdx.x; i < waves * 2 * depth; i += 32) {
         const uint32_t w = i / (2 * depth), k = i - w * 2 * depth;
-        const unsigned long long v = static_cast<unsigned long long>(max(counters[w * 4 * depth + k], 0));
+        const int* c = counters + w * k_batch_counters_per_bounce * depth;
+        const unsigned long long v = static_cast<unsigned long long>(max(c[k], 0));
         if (k < depth) closest += v;
         else shadow += v;
+        redecided += static_cast<unsigned long long>(max(c[4 * depth + k], 0));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         closest += __shfl_xor_sync(0xffffffffu, closest, o);
         shadow += __shfl_xor_sync(0xffffffffu, shadow, o);
+        redecided += __shfl_xor_sync(0xffffffffu, redecided, o);
     }
     if (threadIdx.x == 0) {
         stats[5] += closest;
         stats[6] += shadow;
+        stats[8] += redecided;
     }
 }
 

@@ -279,9 +279,16 @@ __global__ void __launch_bounds__(256) k_leaf_boxes(const float4* __restrict__ t
     if (i >= n) return;
     const uint32_t o = order[i];
     const float4 a = __ldg(&tri_in[3 * o]), b = __ldg(&tri_in[3 * o + 1]), c = __ldg(&tri_in[3 * o + 2]);
-    tris[3 * i] = make_float4(a.x, a.y, a.z, __int_as_float(static_cast<int>(o)));
-    tris[3 * i + 1] = make_float4(__fsub_rn(b.x, a.x), __fsub_rn(b.y, a.y), __fsub_rn(b.z, a.z), 0.f);
-    tris[3 * i + 2] = make_float4(__fsub_rn(c.x, a.x), __fsub_rn(c.y, a.y), __fsub_rn(c.z, a.z), 0.f);
+    {
+        // edges rounded to FP32, and the per-triangle factors of the test's error bound
+        // (robust.cuh) from their 1-norms
+        const float3 e1 = mk3(__fsub_rn(b.x, a.x), __fsub_rn(b.y, a.y), __fsub_rn(b.z, a.z));
+        const float3 e2 = mk3(__fsub_rn(c.x, a.x), __fsub_rn(c.y, a.y), __fsub_rn(c.z, a.z));
+        const float n1 = fabsf(e1.x) + fabsf(e1.y) + fabsf(e1.z), n2 = fabsf(e2.x) + fabsf(e2.y) + fabsf(e2.z);
+        tris[3 * i] = make_float4(a.x, a.y, a.z, __int_as_float(static_cast<int>(o)));
+        tris[3 * i + 1] = make_float4(e1.x, e1.y, e1.z, robust_k1(n1, n2));
+        tris[3 * i + 2] = make_float4(e2.x, e2.y, e2.z, robust_k2(n1, n2));
+    }
     float3 lo = mk3(fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z)));
     float3 hi = mk3(fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z)));
     if (n == 1) {
@@ -392,7 +399,9 @@ __global__ void __launch_bounds__(128) k_collapse8(const float4* __restrict__ no
         wide_entry(nodes, c, 0, e[pick]);
         ++count;
     }
-    // node box, grid origin and scale
+    // node box; the grid covers it padded by the scene's Delta (every child box is quantised
+    // padded by Delta, lower planes rounded down and upper planes up), so a ray's FP32 slab
+    // test never culls a child box the exact ray touches (robust.cuh)
     float lo[3], hi[3];
     for (int a = 0; a < 3; ++a) {
         lo[a] = e[0].lo[a];
@@ -402,10 +411,13 @@ __global__ void __launch_bounds__(128) k_collapse8(const float4* __restrict__ no
             hi[a] = fmaxf(hi[a], e[i].hi[a]);
         }
     }
+    const float pad = scene_box_pad(nodes);
+    float glo[3];
     uint32_t ex[3];
     float inv_s[3];
     for (int a = 0; a < 3; ++a) {
-        ex[a] = wide_exponent(lo[a], hi[a]);
+        glo[a] = __fsub_rd(lo[a], pad);
+        ex[a] = wide_exponent(glo[a], __fadd_ru(hi[a], pad));
         inv_s[a] = __uint_as_float((254u - ex[a]) << 23);  // 2^-e for e in [-100, 126]
     }
     // slots by direction: child i goes to the free slot s maximising sum_a sign_s(a) * c_i(a),
@@ -451,8 +463,8 @@ __global__ void __launch_bounds__(128) k_collapse8(const float4* __restrict__ no
     for (int i = 0; i < count; ++i) {
         const int s = slot_of[i];
         for (int a = 0; a < 3; ++a) {
-            const float ql = floorf(__fmul_rd(__fsub_rd(e[i].lo[a], lo[a]), inv_s[a]));
-            const float qh = ceilf(__fmul_ru(__fsub_ru(e[i].hi[a], lo[a]), inv_s[a]));
+            const float ql = floorf(__fmul_rd(__fsub_rd(__fsub_rd(e[i].lo[a], pad), glo[a]), inv_s[a]));
+            const float qh = ceilf(__fmul_ru(__fsub_ru(__fadd_ru(e[i].hi[a], pad), glo[a]), inv_s[a]));
             const uint32_t bl = static_cast<uint32_t>(fminf(fmaxf(ql, 0.0f), 255.0f));
             const uint32_t bh = static_cast<uint32_t>(fminf(fmaxf(qh, 0.0f), 255.0f));
             qb[a][0][s >> 2] = (qb[a][0][s >> 2] & ~(255u << (8 * (s & 3)))) | (bl << (8 * (s & 3)));
@@ -466,7 +478,7 @@ __global__ void __launch_bounds__(128) k_collapse8(const float4* __restrict__ no
         }
     }
     float4* w = wide + k_wide_node_f4 * static_cast<size_t>(b);
-    w[0] = make_float4(lo[0], lo[1], lo[2], __uint_as_float(ex[0] | (ex[1] << 8) | (ex[2] << 16) | (imask << 24)));
+    w[0] = make_float4(glo[0], glo[1], glo[2], __uint_as_float(ex[0] | (ex[1] << 8) | (ex[2] << 16) | (imask << 24)));
     for (int a = 0; a < 3; ++a)
         w[1 + a] = make_float4(__uint_as_float(qb[a][0][0]), __uint_as_float(qb[a][0][1]), __uint_as_float(qb[a][1][0]),
                                __uint_as_float(qb[a][1][1]));

@@ -20,6 +20,7 @@ __global__ void __launch_bounds__(128) k_megakernel(FrameParams f, SceneDev s, P
     uint32_t e = 0;
     TraceCounters c;
     int rays = 0, shadow_rays = 0;
+    const float pad = s.n_tris ? scene_box_pad(s.nodes) : 0.0f;
     while (true) {
         int base = 0;
         if (lane == 0) base = atomicAdd(fetch, 32);
@@ -35,7 +36,7 @@ __global__ void __launch_bounds__(128) k_megakernel(FrameParams f, SceneDev s, P
         float4 aa = make_float4(0.f, 0.f, 0.f, 0.f), an = aa;
         uint32_t sig = 0;
         const float3 L =
-            trace_path<STATS>(f, s, x, y, f.sample_base + j, nullptr, nv, &aa, &an, &sig, e, c, rays, shadow_rays);
+            trace_path<STATS>(f, s, x, y, f.sample_base + j, nullptr, nv, &aa, &an, &sig, e, c, rays, shadow_rays, pad);
         p.lpath[gid] = make_float4(L.x, L.y, L.z, 0.f);
         p.aov_a[gid] = aa;
         p.aov_n[gid] = an;
@@ -69,6 +70,7 @@ __global__ void __launch_bounds__(128) k_adjoint(FrameParams f, SceneDev s, cons
     uint32_t e = 0;
     TraceCounters c;
     int rays = 0;
+    const float pad = s.n_tris ? scene_box_pad(s.nodes) : 0.0f;
     while (true) {
         int base = 0;
         if (lane == 0) base = atomicAdd(fetch, 32);
@@ -84,7 +86,7 @@ __global__ void __launch_bounds__(128) k_adjoint(FrameParams f, SceneDev s, cons
         const float3 d = mk3(grad_image[3 * px] * inv_spp, grad_image[3 * px + 1] * inv_spp,
                              grad_image[3 * px + 2] * inv_spp);
         if (d.x == 0.0f && d.y == 0.0f && d.z == 0.0f) continue;
-        adjoint_path(f, s, x, y, f.sample_base + j, d, grad_albedo, grad_emission, e, c, rays);
+        adjoint_path(f, s, x, y, f.sample_base + j, d, grad_albedo, grad_emission, e, c, rays, pad);
     }
     if (e) atomicOr(err, e);
     warp_add_count(rays, &stats[7]);

@@ -61,10 +61,20 @@ __device__ __forceinline__ const float4* stage_treelet(const SceneDev& s) {
 struct PathDev {
     float4* beta;
     float4* lpath;
-    float4* aov_a;   // first-hit albedo (rgb) + depth (w)
-    float4* aov_n;   // first-hit remapped normal
-    float4* ray_ff;  // 3 float4 per path: the double-float ray of the path's next segment
-    uint32_t* sig;   // path signatures (record mode) or null
+    float4* aov_a;      // first-hit albedo (rgb) + depth (w)
+    float4* aov_n;      // first-hit remapped normal
+    float4* ray_ff;     // 3 float4 per path: the double-float ray of the path's next segment
+    uint32_t* sig;      // path signatures (record mode) or null
+    float4* shadow_ff;  // 3 float4 per path: the exact shadow segment of the current vertex
+                        // (start, end - start in double-float), for exact re-decisions
+};
+
+// List of rays a fast trace kernel could not decide for certain (robust.cuh); the fixup
+// kernel re-traces them with exact re-decisions.
+struct DeferList {
+    int* list;
+    int* count;
+    __device__ __forceinline__ void push(int i) const { list[atomicAdd(count, 1)] = i; }
 };
 
 // Pixel slots are ordered in 8x4 tiles so a warp's camera rays cover a compact patch.
@@ -149,11 +159,16 @@ __device__ __forceinline__ bool begin_path(const FrameParams& f, const PathDev& 
 }
 
 // Closest-hit queue: ray i is q[2i] = (origin, path id), q[2i+1] = (direction, excluded
-// triangle); the result is hits[i] = (t, triangle or -1, u, v).
+// triangle); the result is hits[i] = (t, triangle or -1, u, v). The exact ray of path pid is
+// ray_ff[3 pid] (the path's double-float segment).
 struct ClosestJob {
     const float4* __restrict__ q;
     float4* __restrict__ hits;
+    const float4* __restrict__ ray_ff;
+    DeferList deferred;
     __device__ __forceinline__ int pid(int i) const { return __float_as_int(q[2 * i].w); }
+    __device__ __forceinline__ ExactPtr exact(int i) const { return ExactPtr{ray_ff + 3ull * pid(i)}; }
+    __device__ __forceinline__ void defer(int i) const { deferred.push(i); }
     __device__ __forceinline__ void load(int i, float3& o, float3& d, float& tmax, int& exclude) const {
         const float4 r0 = q[2 * i], r1 = q[2 * i + 1];
         o = xyz(r0);
@@ -161,17 +176,21 @@ struct ClosestJob {
         tmax = __int_as_float(0x7f800000);
         exclude = __float_as_int(r1.w);
     }
-    __device__ __forceinline__ void store(int i, const TraceState& s) const {
-        hits[i] = make_float4(s.best_t, __int_as_float(s.best), s.bu, s.bv);
+    __device__ __forceinline__ void store(int i, const TraceResult& s) const {
+        hits[i] = make_float4(s.t, __int_as_float(s.prim), s.u, s.v);
     }
 };
 
 // Shadow queue: sq[3i] = (origin, path id), sq[3i+1] = (direction, t_max), sq[3i+2] =
-// (contribution); an unoccluded ray adds its contribution to the path's radiance.
+// (contribution); an unoccluded ray adds its contribution to the path's radiance. The exact
+// segment of path pid is p.shadow_ff[3 pid].
 struct ShadowJob {
     const float4* __restrict__ sq;
     PathDev p;
+    DeferList deferred;
     __device__ __forceinline__ int pid(int i) const { return __float_as_int(sq[3 * i].w); }
+    __device__ __forceinline__ ExactPtr exact(int i) const { return ExactPtr{p.shadow_ff + 3ull * pid(i)}; }
+    __device__ __forceinline__ void defer(int i) const { deferred.push(i); }
     __device__ __forceinline__ void load(int i, float3& o, float3& d, float& tmax, int& exclude) const {
         const float4 r0 = sq[3 * i], r1 = sq[3 * i + 1];
         o = xyz(r0);
@@ -179,9 +198,9 @@ struct ShadowJob {
         tmax = r1.w;
         exclude = -1;
     }
-    __device__ __forceinline__ void store(int i, const TraceState& s) const {
+    __device__ __forceinline__ void store(int i, const TraceResult& s) const {
         const int pid = __float_as_int(sq[3 * i].w);
-        if (s.best < 0) {
+        if (s.prim < 0) {
             const float4 c = sq[3 * i + 2];
             float4 L = p.lpath[pid];
             L.x += c.x;
@@ -189,7 +208,7 @@ struct ShadowJob {
             L.z += c.z;
             p.lpath[pid] = L;
         }
-        if (p.sig) p.sig[pid] = sig_mix(p.sig[pid], s.best < 0 ? k_sig_lit : k_sig_shadowed);
+        if (p.sig) p.sig[pid] = sig_mix(p.sig[pid], s.prim < 0 ? k_sig_lit : k_sig_shadowed);
     }
 };
 
@@ -237,6 +256,7 @@ __device__ __forceinline__ void shade_hit(const FrameParams& f, const SceneDev& 
     }
     o.shadow = v.nee;
     if (v.nee) {
+        ff_ray_store(&p.shadow_ff[3ull * pid], v.seg_o, v.seg_d);
         o.contrib = beta * alb * xyz(__ldg(&s.emission[v.light])) * v.g;
         o.so = v.so;
         o.sd = v.sd;
@@ -317,12 +337,14 @@ struct PathVertex {
 // their rays; the binary LBVH traversal (fewer registers) is the faster one in that form:
 // the 10k-triangle adjoint took 5.5 ms with it and 7.2 ms with the 8-wide records on GB300.
 // Returns the radiance; writes first-hit AOVs and the signature when the pointers are set.
-// rays / shadow_rays are incremented per closest-hit / shadow ray traced.
+// rays / shadow_rays are incremented per closest-hit / shadow ray traced. Hit decisions are
+// exact (robust traversal, re-deciding undecided candidates inline from the path's
+// double-float geometry); pad is the scene's box padding (scene_box_pad).
 template <bool STATS>
 __device__ __forceinline__ float3 trace_path(const FrameParams& f, const SceneDev& s, uint32_t x, uint32_t y,
                                              uint32_t sample, PathVertex* verts, int& n_verts, float4* aov_a,
                                              float4* aov_n, uint32_t* sig_out, uint32_t& err, TraceCounters& cnt,
-                                             int& rays, int& shadow_rays) {
+                                             int& rays, int& shadow_rays, float pad) {
     const VertexScene vs{s.tri_in, s.tri_nrm, s.albedo, s.emission, s.emitters, s.n_emit, f.eps};
     ff3 ro, rd;
     camera_ray_ff(f, x, y, sample, ro, rd);
@@ -331,11 +353,12 @@ __device__ __forceinline__ float3 trace_path(const FrameParams& f, const SceneDe
     int exclude = -1;
     n_verts = 0;
     for (uint32_t k = 1; k <= f.max_depth; ++k) {
-        const RayInv r = make_ray(ff3_f(ro), ff3_f(rd));
+        const RayInv r = make_ray(ff3_f(ro), ff3_f(rd), pad);
         float t, bu, bv;
         ++rays;
-        const int prim = trace_bvh<false, STATS>(s.nodes, s.tris, s.n_tris, r, __int_as_float(0x7f800000), exclude, t,
-                                                 bu, bv, err, cnt);
+        const int prim = trace_bvh<false, STATS, false, true>(s.nodes, s.tris, s.tri_in, s.n_tris, r,
+                                                              __int_as_float(0x7f800000), exclude, t, bu, bv, err, cnt,
+                                                              ExactRegs{ro, rd});
         if (prim < 0) {
             sig = sig_mix(sig, k_sig_miss);
             break;
@@ -354,10 +377,11 @@ __device__ __forceinline__ float3 trace_path(const FrameParams& f, const SceneDe
         }
         float gv = 0.0f;
         if (v.nee) {
-            const RayInv sr = make_ray(v.so, v.sd);
+            const RayInv sr = make_ray(v.so, v.sd, pad);
             float st2, su, sv;
             ++shadow_rays;
-            const int occ = trace_bvh<true, STATS>(s.nodes, s.tris, s.n_tris, sr, v.stmax, -1, st2, su, sv, err, cnt);
+            const int occ = trace_bvh<true, STATS, false, true>(s.nodes, s.tris, s.tri_in, s.n_tris, sr, v.stmax, -1,
+                                                                st2, su, sv, err, cnt, ExactRegs{v.seg_o, v.seg_d});
             if (occ < 0) {
                 // The same product and the same unfused add as the wavefront's shadow kernel.
                 const float3 cb = beta * alb * xyz(__ldg(&s.emission[v.light])) * v.g;
@@ -396,11 +420,11 @@ __device__ __forceinline__ float3 trace_path(const FrameParams& f, const SceneDe
 __device__ __forceinline__ void adjoint_path(const FrameParams& f, const SceneDev& s, uint32_t x, uint32_t y,
                                              uint32_t sample, float3 d, float* __restrict__ grad_albedo,
                                              float* __restrict__ grad_emission, uint32_t& err, TraceCounters& cnt,
-                                             int& rays) {
+                                             int& rays, float pad) {
     PathVertex verts[k_adjoint_max_depth];
     float3 H[k_adjoint_max_depth];
     int nv = 0, shadow_rays = 0;
-    trace_path<false>(f, s, x, y, sample, verts, nv, nullptr, nullptr, nullptr, err, cnt, rays, shadow_rays);
+    trace_path<false>(f, s, x, y, sample, verts, nv, nullptr, nullptr, nullptr, err, cnt, rays, shadow_rays, pad);
     rays += shadow_rays;
     nv = min(nv, k_adjoint_max_depth);
     if (nv == 0) return;

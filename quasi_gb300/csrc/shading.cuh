@@ -39,6 +39,7 @@ struct VertexResult {
     float g;           // NEE factor: contribution = beta * albedo * emission(light) * g
     float3 so, sd;     // shadow ray origin and unit direction (float)
     float stmax;       // shadow ray t_max
+    ff3 seg_o, seg_d;  // the exact shadow segment: start and end - start (double-float)
     ff3 org;           // continuation origin x + eps n (double-float)
     ff3 dir;           // continuation direction (valid when want_dir)
 };
@@ -127,7 +128,9 @@ __device__ __forceinline__ void shade_vertex(const VertexScene& s, uint32_t key,
                 // neither end's plane (nor a coplanar neighbour) can be crossed.
                 const float side = cl < 0.0f ? s.eps : -s.eps;
                 const ff3 so = ff3_add(yl, ff3_scale(nl, side));
-                const float3 sd = ff3_f(ff3_sub(out.org, so));
+                out.seg_o = so;
+                out.seg_d = ff3_sub(out.org, so);
+                const float3 sd = ff3_f(out.seg_d);
                 const float sdist = __fsqrt_rn(fdot3(sd, sd));
                 const float inv_s = __fdiv_rn(1.0f, sdist);
                 out.so = ff3_f(so);

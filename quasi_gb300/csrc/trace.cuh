@@ -8,6 +8,10 @@
 //
 // Closest hit is defined independently of traversal order: the smallest t wins and an
 // exact tie goes to the smaller original triangle index. The oracle uses the same rule.
+// Hit decisions agree with exact arithmetic (robust.cuh): every FP32 triangle test carries
+// an error bound, boxes are padded by more than the slab planes' rounding, and box tests
+// cull beyond the closest hit's t plus its error bound. Undecided candidates either flag
+// the ray for the fixup kernel (fast mode) or are re-decided in double-float (ROBUST).
 //
 // Traversal is written as a resumable step (one node visit) so persistent kernels can keep
 // every lane of a warp busy: a lane whose ray finishes takes a new ray from the queue while
@@ -15,6 +19,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "robust.cuh"
 
 namespace quasi {
 
@@ -30,11 +35,28 @@ constexpr int k_trace_steps = 8;
 // block) 22% slower; the top levels are L1-resident either way.
 constexpr int k_default_smem_levels = 5;
 
+// Undecided-candidate marker in a trace result (fast mode): the ray is re-traced by the
+// fixup kernel with exact re-decisions.
+constexpr int k_prim_flagged = -2;
+
+// Spatial box padding Delta of the scene whose binary LBVH is `nodes`: 2^-16 times the
+// largest absolute vertex coordinate S (the root's child boxes hold every vertex). The
+// 8-wide records are padded by the same Delta when they are built (k_collapse8); the binary
+// traversal pads its slab planes per ray.
+__device__ __forceinline__ float scene_box_pad(const float4* __restrict__ nodes) {
+    const float4 n0 = __ldg(&nodes[0]), n1 = __ldg(&nodes[1]), n2 = __ldg(&nodes[2]);
+    const float sxy = fmaxf(fmaxf(fmaxf(fabsf(n0.x), fabsf(n0.y)), fmaxf(fabsf(n0.z), fabsf(n0.w))),
+                            fmaxf(fmaxf(fabsf(n1.x), fabsf(n1.y)), fmaxf(fabsf(n1.z), fabsf(n1.w))));
+    const float sz = fmaxf(fmaxf(fabsf(n2.x), fabsf(n2.y)), fmaxf(fabsf(n2.z), fabsf(n2.w)));
+    return __fmul_rn(fmaxf(fmaxf(sxy, sz), 0x1p-100f), k_box_pad_rel);
+}
+
 struct RayInv {
     float3 o;
     float3 d;
-    float3 inv;  // 1/d with tiny components clamped away from zero
-    float3 oinv; // o * inv
+    float3 inv;     // 1/d with tiny components clamped away from zero
+    float3 oinv_lo; // (o + pad) * inv: lower slab planes moved out by pad
+    float3 oinv_hi; // (o - pad) * inv: upper slab planes moved out by pad
 };
 
 __device__ __forceinline__ float safe_inv(float x) {
@@ -42,75 +64,112 @@ __device__ __forceinline__ float safe_inv(float x) {
     return 1.0f / ax;
 }
 
-__device__ __forceinline__ RayInv make_ray(float3 o, float3 d) {
+// pad: spatial box padding (scene_box_pad); 0 for the 8-wide records, which carry it.
+__device__ __forceinline__ RayInv make_ray(float3 o, float3 d, float pad = 0.0f) {
     RayInv r;
     r.o = o;
     r.d = d;
     r.inv = mk3(safe_inv(d.x), safe_inv(d.y), safe_inv(d.z));
-    r.oinv = mk3(o.x * r.inv.x, o.y * r.inv.y, o.z * r.inv.z);
+    r.oinv_lo = mk3((o.x + pad) * r.inv.x, (o.y + pad) * r.inv.y, (o.z + pad) * r.inv.z);
+    r.oinv_hi = mk3((o.x - pad) * r.inv.x, (o.y - pad) * r.inv.y, (o.z - pad) * r.inv.z);
     return r;
 }
 
-// Slab test of one child box; returns entry distance, or +inf on a miss.
+// Slab test of one child box padded by the ray's pad; returns entry distance, or +inf.
 __device__ __forceinline__ float box_entry(const RayInv& r, float lox, float hix, float loy, float hiy, float loz,
                                            float hiz, float tmax) {
-    const float tx0 = fmaf(lox, r.inv.x, -r.oinv.x), tx1 = fmaf(hix, r.inv.x, -r.oinv.x);
-    const float ty0 = fmaf(loy, r.inv.y, -r.oinv.y), ty1 = fmaf(hiy, r.inv.y, -r.oinv.y);
-    const float tz0 = fmaf(loz, r.inv.z, -r.oinv.z), tz1 = fmaf(hiz, r.inv.z, -r.oinv.z);
+    const float tx0 = fmaf(lox, r.inv.x, -r.oinv_lo.x), tx1 = fmaf(hix, r.inv.x, -r.oinv_hi.x);
+    const float ty0 = fmaf(loy, r.inv.y, -r.oinv_lo.y), ty1 = fmaf(hiy, r.inv.y, -r.oinv_hi.y);
+    const float tz0 = fmaf(loz, r.inv.z, -r.oinv_lo.z), tz1 = fmaf(hiz, r.inv.z, -r.oinv_hi.z);
     const float tmin = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.0f));
     const float tfar = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
     return tmin <= tfar * k_box_pad ? tmin : __int_as_float(0x7f800000);
 }
 
-// Moller & Trumbore (1997) with precomputed edges. Returns t or +inf, and the barycentrics
-// (u, v) of the hit, from which the hit point is rebuilt as v0 + u e1 + v e2 (on the
-// triangle's plane to within vertex rounding, unlike o + t d).
-__device__ __forceinline__ float tri_t(const RayInv& r, float4 a, float4 e1, float4 e2, float& u, float& v) {
-    const float3 E1 = xyz(e1), E2 = xyz(e2);
-    const float3 p = cross(r.d, E2);
-    const float det = dot(E1, p);
-    const float inv = 1.0f / det;  // det == 0 gives inf/nan and fails the tests below
-    const float3 tv = r.o - xyz(a);
-    u = dot(tv, p) * inv;
-    const float3 q = cross(tv, E1);
-    v = dot(r.d, q) * inv;
-    const float t = dot(E2, q) * inv;
-    const bool ok = (u >= 0.0f) && (v >= 0.0f) && (u + v <= 1.0f) && (t > 0.0f) && (det != 0.0f);
-    return ok ? t : __int_as_float(0x7f800000);
+// Start of a closest-hit (t_max = inf) or any-hit (t_max of the segment) query.
+__device__ __forceinline__ HitBest hit_begin(float tmax) {
+    HitBest b;
+    b.t = tmax;
+    // t_max of a shadow segment is FP32 (its length times 1 - 1e-4, a few roundings)
+    b.dt = tmax < __int_as_float(0x7f800000) ? 8.0f * k_ulp * tmax : 0.0f;
+    b.prim = -1;
+    b.u = b.v = 0.0f;
+    return b;
 }
+
+// Tests the triangle at leaf position `pos` (tris: leaf order {v0, orig}, {e1, K1},
+// {e2, K2}; tri_in: original-order vertices for re-decisions) and updates `b`. Returns true
+// when the traversal ends: an any-hit query is answered, or (fast mode) an undecided
+// candidate marks the result k_prim_flagged for the fixup kernel.
+template <bool ANY, bool ROBUST, class X>
+__device__ __forceinline__ bool leaf_test(const float4* __restrict__ tris, const float4* __restrict__ tri_in,
+                                          const X& xr, const RayInv& r, uint32_t pos, int exclude, HitBest& b) {
+    const float4* p = tris + 3ull * pos;
+    const float4 a = __ldg(p), e1 = __ldg(p + 1), e2 = __ldg(p + 2);
+    const int orig = __float_as_int(a.w);
+    if (orig == exclude) return false;
+    float t, dt, u, v;
+    const int c = tri_classify<ANY>(r.o, r.d, a, e1, e2, t, dt, u, v);
+    if (c == k_tri_miss) return false;
+    if (c == k_tri_hit) {
+        if (t + dt < b.t - b.dt) {  // certainly closer than the closest so far (inside t_max)
+            b.t = t;
+            b.dt = dt;
+            b.prim = orig;
+            b.u = u;
+            b.v = v;
+            return ANY;
+        }
+        if (t - dt > b.t + b.dt) return false;  // certainly farther
+    }
+    if constexpr (ROBUST) {
+        return redecide<ANY>(tri_in, xr, orig, b);
+    } else {
+        b.prim = k_prim_flagged;
+        return true;
+    }
+}
+
+// No exact geometry (fast mode never re-decides).
+struct ExactNone {
+    __device__ __forceinline__ void get(ff3&, ff3&) const {}
+};
 
 struct TraceCounters {
     uint32_t nodes = 0;
     uint32_t tris = 0;
 };
 
-// Per-ray traversal state; the stack lives beside it (thread-local array).
+// Result of one traversal: prim = original index of the closest hit, -1 for none, or
+// k_prim_flagged (fast mode: re-trace in the fixup kernel).
+struct TraceResult {
+    float t;
+    int prim;
+    float u, v;
+};
+__device__ __forceinline__ TraceResult trace_result(const HitBest& b) { return TraceResult{b.t, b.prim, b.u, b.v}; }
+
+// Per-ray traversal state of the resumable binary traversal (the stack lives beside it).
 struct TraceState {
     RayInv r;
-    float tmax;
     int exclude;
-    float best_t;
-    int best;  // original index of the closest hit so far, or -1
-    float bu, bv;
+    HitBest b;
     int node;
     int sp;
     uint32_t budget;
 };
 
 __device__ __forceinline__ void trace_begin(TraceState& s, float3 o, float3 d, float tmax, int exclude,
-                                            uint32_t n_tris) {
-    s.r = make_ray(o, d);
-    s.tmax = tmax;
+                                            uint32_t n_tris, float pad) {
+    s.r = make_ray(o, d, pad);
     s.exclude = exclude;
-    s.best_t = tmax;
-    s.best = -1;
-    s.bu = s.bv = 0.0f;
+    s.b = hit_begin(tmax);
     s.node = n_tris == 0 ? -1 : 0;
     s.sp = 0;
     s.budget = 2u * n_tris + 64u;
 }
 
-// One node visit. Returns true when the traversal has finished (state holds the result).
+// One node visit (fast mode). Returns true when the traversal has finished.
 template <bool ANY, bool STATS>
 __device__ __forceinline__ bool trace_step(const float4* __restrict__ nodes, const float4* __restrict__ tris,
                                            TraceState& s, int* stack, uint32_t& err, TraceCounters& cnt) {
@@ -124,37 +183,26 @@ __device__ __forceinline__ bool trace_step(const float4* __restrict__ nodes, con
     const float4 n1 = __ldg(&nodes[4 * s.node + 1]);
     const float4 n2 = __ldg(&nodes[4 * s.node + 2]);
     const float4 n3 = __ldg(&nodes[4 * s.node + 3]);
-    const float t0 = box_entry(s.r, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, s.best_t);
-    const float t1 = box_entry(s.r, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, s.best_t);
+    const float tcull = s.b.t + s.b.dt;
+    const float t0 = box_entry(s.r, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, tcull);
+    const float t1 = box_entry(s.r, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, tcull);
     const int c0 = __float_as_int(n3.x);
     const int c1 = __float_as_int(n3.y);
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
         const int c = k == 0 ? c0 : c1;
         const float tb = k == 0 ? t0 : t1;
-        if (c < 0 && tb < s.best_t) {
-            const int pos = ~c;
+        if (c < 0 && tb < s.b.t + s.b.dt) {
             if (STATS) ++cnt.tris;
-            const float4 a = __ldg(&tris[3 * pos]);
-            const float4 e1 = __ldg(&tris[3 * pos + 1]);
-            const float4 e2 = __ldg(&tris[3 * pos + 2]);
-            const int orig = __float_as_int(a.w);
-            float u, v;
-            const float t = tri_t(s.r, a, e1, e2, u, v);
-            if (orig != s.exclude && (t < s.best_t || (t == s.best_t && orig < s.best && t < s.tmax))) {
-                s.best_t = t;
-                s.best = orig;
-                s.bu = u;
-                s.bv = v;
-                if (ANY) {
-                    s.node = -1;
-                    return true;
-                }
+            if (leaf_test<ANY, false>(tris, nullptr, ExactNone{}, s.r, ~c, s.exclude, s.b)) {
+                s.node = -1;
+                return true;
             }
         }
     }
-    const bool h0 = c0 >= 0 && t0 < s.best_t;
-    const bool h1 = c1 >= 0 && t1 < s.best_t;
+    const float tc = s.b.t + s.b.dt;
+    const bool h0 = c0 >= 0 && t0 < tc;
+    const bool h1 = c1 >= 0 && t1 < tc;
     if (h0 && h1) {
         const bool swap = t1 < t0;
         if (s.sp >= k_stack_size) {
@@ -180,8 +228,9 @@ __device__ __forceinline__ bool trace_step(const float4* __restrict__ nodes, con
 
 // Whole-ray traversal for kernels that trace one ray at a time.
 // ANY = true: stops at the first hit with t in (0, tmax) and returns a prim >= 0.
-// Returns the original index of the hit triangle (or -1), its distance in t_out and its
-// barycentrics in bu, bv.
+// Returns the original index of the hit triangle (or -1; k_prim_flagged in fast mode when an
+// undecided candidate was met), its distance in t_out and its barycentrics in bu, bv.
+// ROBUST: undecided candidates are re-decided exactly from xr (exact ray) and tri_in.
 // Treelet nodes (the top levels copied to shared memory) are addressed as k_tree_flag | i.
 constexpr int k_tree_flag = 0x40000000;
 
@@ -189,16 +238,16 @@ constexpr int k_tree_flag = 0x40000000;
 // GB300 than driving trace_step in a loop, so the batch-fetch kernels use it. With tree_n > 0
 // the traversal starts in `tree` (shared memory), whose child links point into the treelet
 // (k_tree_flag) or out to global nodes.
-template <bool ANY, bool STATS, bool TREE = false>
+template <bool ANY, bool STATS, bool TREE = false, bool ROBUST = false, class X = ExactNone>
 __device__ __forceinline__ int trace_bvh(const float4* __restrict__ nodes, const float4* __restrict__ tris,
-                                         uint32_t n_tris, const RayInv& r, float tmax, int exclude, float& t_out,
-                                         float& bu, float& bv, uint32_t& err, TraceCounters& cnt,
-                                         const float4* tree = nullptr, int tree_n = 0) {
-    float best_t = tmax;
-    int best = -1;
-    bu = bv = 0.0f;
+                                         const float4* __restrict__ tri_in, uint32_t n_tris, const RayInv& r,
+                                         float tmax, int exclude, float& t_out, float& bu, float& bv, uint32_t& err,
+                                         TraceCounters& cnt, const X& xr = X{}, const float4* tree = nullptr,
+                                         int tree_n = 0) {
+    HitBest b = hit_begin(tmax);
     if (n_tris == 0) {
-        t_out = best_t;
+        t_out = b.t;
+        bu = bv = 0.0f;
         return -1;
     }
     int stack[k_stack_size];
@@ -224,37 +273,25 @@ __device__ __forceinline__ int trace_bvh(const float4* __restrict__ nodes, const
             n2 = __ldg(&nodes[4 * node + 2]);
             n3 = __ldg(&nodes[4 * node + 3]);
         }
-        float t0 = box_entry(r, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, best_t);
-        float t1 = box_entry(r, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, best_t);
+        const float tcull = b.t + b.dt;
+        float t0 = box_entry(r, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, tcull);
+        float t1 = box_entry(r, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, tcull);
         int c0 = __float_as_int(n3.x);
         int c1 = __float_as_int(n3.y);
+        bool ended = false;
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
             const int c = k == 0 ? c0 : c1;
             const float tb = k == 0 ? t0 : t1;
-            if (c < 0 && tb < best_t) {
-                const int pos = ~c;
+            if (!ended && c < 0 && tb < b.t + b.dt) {
                 if (STATS) ++cnt.tris;
-                const float4 a = __ldg(&tris[3 * pos]);
-                const float4 e1 = __ldg(&tris[3 * pos + 1]);
-                const float4 e2 = __ldg(&tris[3 * pos + 2]);
-                const int orig = __float_as_int(a.w);
-                float u, v;
-                const float t = tri_t(r, a, e1, e2, u, v);
-                if (orig != exclude && (t < best_t || (t == best_t && orig < best && t < tmax))) {
-                    best_t = t;
-                    best = orig;
-                    bu = u;
-                    bv = v;
-                    if (ANY) {
-                        t_out = best_t;
-                        return best;
-                    }
-                }
+                ended = leaf_test<ANY, ROBUST>(tris, tri_in, xr, r, ~c, exclude, b);
             }
         }
-        const bool h0 = c0 >= 0 && t0 < best_t;
-        const bool h1 = c1 >= 0 && t1 < best_t;
+        if (ended) break;
+        const float tc = b.t + b.dt;
+        const bool h0 = c0 >= 0 && t0 < tc;
+        const bool h1 = c1 >= 0 && t1 < tc;
         if (h0 && h1) {
             int near_c = c0, far_c = c1;
             if (t1 < t0) {
@@ -276,19 +313,34 @@ __device__ __forceinline__ int trace_bvh(const float4* __restrict__ nodes, const
             node = stack[--sp];
         }
     }
-    t_out = best_t;
-    return best;
+    t_out = b.t;
+    bu = b.u;
+    bv = b.v;
+    return b.prim;
+}
+
+// Hands one finished ray to the job: a flagged ray goes to the fixup list, others store.
+template <class Job>
+__device__ __forceinline__ void finish_ray(Job& job, int i, const TraceResult& res) {
+    if (res.prim == k_prim_flagged)
+        job.defer(i);
+    else
+        job.store(i, res);
 }
 
 // Warp-batch persistent traversal: a warp takes 32 consecutive rays with one atomic and
 // traces them to completion before taking more (coherent node fetches within a batch).
-// tree/tree_n: the treelet in shared memory (used when TREE).
+// tree/tree_n: the treelet in shared memory (used when TREE). Job supplies
+//   void load(int i, float3& o, float3& d, float& tmax, int& exclude)
+//   void store(int i, const TraceResult& r)
+//   void defer(int i)        (the ray met an undecided candidate: re-trace it exactly)
 template <bool ANY, bool STATS, bool TREE, class Job>
 __device__ __forceinline__ void trace_batches(Job& job, const float4* __restrict__ nodes,
                                               const float4* __restrict__ tris, uint32_t n_tris, int n,
                                               int* __restrict__ fetch, uint32_t& err, TraceCounters& cnt,
                                               const float4* tree, int tree_n) {
     const int lane = threadIdx.x & 31;
+    const float pad = n_tris ? scene_box_pad(nodes) : 0.0f;
     while (true) {
         int base = 0;
         if (lane == 0) base = atomicAdd(fetch, 32);
@@ -300,29 +352,27 @@ __device__ __forceinline__ void trace_batches(Job& job, const float4* __restrict
             float tmax;
             int exclude;
             job.load(i, o, d, tmax, exclude);
-            TraceState s;
-            s.r = make_ray(o, d);
-            s.tmax = tmax;
-            s.best = trace_bvh<ANY, STATS, TREE>(nodes, tris, n_tris, s.r, tmax, exclude, s.best_t, s.bu, s.bv, err,
-                                                 cnt, tree, tree_n);
-            job.store(i, s);
+            const RayInv r = make_ray(o, d, pad);
+            TraceResult res;
+            res.prim = trace_bvh<ANY, STATS, TREE>(nodes, tris, nullptr, n_tris, r, tmax, exclude, res.t, res.u, res.v,
+                                                   err, cnt, ExactNone{}, tree, tree_n);
+            finish_ray(job, i, res);
         }
     }
 }
 
 // Persistent traversal of a queue of n rays with per-lane refill: once `refill` lanes of a
 // warp are idle they take the next rays with one atomic (refill = 32 takes 32 rays at a
-// time and waits for all of them). Job supplies
-//   void load(int i, float3& o, float3& d, float& tmax, int& exclude)
-//   void store(int i, const TraceState& s)
-// Every lane of the warp must call this (it uses full-warp votes).
-// Between refills each lane runs up to `steps` node visits without warp votes.
+// time and waits for all of them). Job as in trace_batches. Every lane of the warp must call
+// this (it uses full-warp votes). Between refills each lane runs up to `steps` node visits
+// without warp votes.
 template <bool ANY, bool STATS, class Job>
 __device__ __forceinline__ void trace_persistent(Job& job, const float4* __restrict__ nodes,
                                                  const float4* __restrict__ tris, uint32_t n_tris, int n, int refill,
                                                  int steps, int* __restrict__ fetch, uint32_t& err,
                                                  TraceCounters& cnt) {
     const int lane = threadIdx.x & 31;
+    const float pad = n_tris ? scene_box_pad(nodes) : 0.0f;
     TraceState s;
     int stack[k_stack_size];
     bool active = false;
@@ -343,7 +393,7 @@ __device__ __forceinline__ void trace_persistent(Job& job, const float4* __restr
                     float tmax;
                     int exclude;
                     job.load(idx, o, d, tmax, exclude);
-                    trace_begin(s, o, d, tmax, exclude, n_tris);
+                    trace_begin(s, o, d, tmax, exclude, n_tris, pad);
                     active = true;
                 }
             }
@@ -351,9 +401,41 @@ __device__ __forceinline__ void trace_persistent(Job& job, const float4* __restr
         if (!__any_sync(0xffffffffu, active)) break;
         for (int k = 0; k < steps && active; ++k) {
             if (trace_step<ANY, STATS>(nodes, tris, s, stack, err, cnt)) {
-                job.store(idx, s);
+                finish_ray(job, idx, trace_result(s.b));
                 active = false;
             }
+        }
+    }
+}
+
+// Re-traces the rays a fast trace kernel deferred (list[0 .. *count)) with exact
+// re-decisions over the binary LBVH, one ray per thread, warps taking 32 list entries per
+// atomic. Job supplies load, store and exact(i) (the ray's exact geometry).
+template <bool ANY, class Job>
+__device__ __forceinline__ void trace_fixups(Job& job, const float4* __restrict__ nodes,
+                                             const float4* __restrict__ tris, const float4* __restrict__ tri_in,
+                                             uint32_t n_tris, const int* __restrict__ list, int n,
+                                             int* __restrict__ fetch, uint32_t& err) {
+    const int lane = threadIdx.x & 31;
+    const float pad = n_tris ? scene_box_pad(nodes) : 0.0f;
+    TraceCounters cnt;
+    while (true) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(fetch, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const int k = base + lane;
+        if (k < n) {
+            const int i = list[k];
+            float3 o, d;
+            float tmax;
+            int exclude;
+            job.load(i, o, d, tmax, exclude);
+            const RayInv r = make_ray(o, d, pad);
+            TraceResult res;
+            res.prim = trace_bvh<ANY, false, false, true>(nodes, tris, tri_in, n_tris, r, tmax, exclude, res.t, res.u,
+                                                          res.v, err, cnt, job.exact(i));
+            job.store(i, res);
         }
     }
 }

@@ -74,7 +74,8 @@ Renderer::~Renderer() {
     bvh_.release();
     for (DeviceBuffer* b : {&raw_vertices_, &tri_in_, &albedo_, &emission_, &emitters_, &quads_, &accum_, &comp_,
                             &aov_albedo_, &aov_normal_, &record_rad_, &record_sig_, &queue_[0], &queue_[1], &hits_,
-                            &shadow_, &beta_, &lpath_, &aov_a_, &aov_n_, &sig_, &ray_ff_, &counters_, &stats_dev_, &err_dev_})
+                            &shadow_, &beta_, &lpath_, &aov_a_, &aov_n_, &sig_, &ray_ff_, &shadow_ff_, &defer_,
+                            &counters_, &stats_dev_, &err_dev_})
         b->release();
     if (counters_host_) cudaFreeHost(counters_host_);
     if (stats_host_) cudaFreeHost(stats_host_);
@@ -247,8 +248,9 @@ int Renderer::ensure_frame_buffers(uint32_t w, uint32_t h) {
 }
 
 // Bytes of wave state per path slot: two ray queues (2 x 32), hit 16, shadow ray 48, beta,
-// radiance and two AOVs (4 x 16), signature 4, double-float ray 48.
-constexpr size_t k_wave_bytes_per_path = 244;
+// radiance and two AOVs (4 x 16), signature 4, double-float ray 48, exact shadow segment 48,
+// fixup list entry 4.
+constexpr size_t k_wave_bytes_per_path = 296;
 
 int Renderer::ensure_wave_buffers(uint32_t paths) {
     if (paths <= wave_capacity_) return QUASI_OK;
@@ -262,6 +264,8 @@ int Renderer::ensure_wave_buffers(uint32_t paths) {
     R_TRY(aov_n_.reserve(sizeof(float4) * paths), "aov");
     R_TRY(sig_.reserve(sizeof(uint32_t) * paths), "sig");
     R_TRY(ray_ff_.reserve(sizeof(float4) * 3ull * paths), "ray_ff");
+    R_TRY(shadow_ff_.reserve(sizeof(float4) * 3ull * paths), "shadow_ff");
+    R_TRY(defer_.reserve(sizeof(int) * paths), "defer");
     wave_capacity_ = paths;
     return QUASI_OK;
 }
@@ -341,7 +345,7 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
     const uint32_t waves = ceil_div(spp, S);
     int rc = ensure_wave_buffers(slots * S);
     if (rc) return rc;
-    const uint32_t per_wave = 4 * D;
+    const uint32_t per_wave = k_counters_per_bounce * D;
     const uint32_t need = per_wave * waves;
     if (need > counter_capacity_) {
         R_TRY(counters_.reserve(sizeof(int) * need), "counters");
@@ -368,7 +372,8 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
                 bv.tri_nrm};
     const size_t tree_smem = sizeof(float4) * 4 * static_cast<size_t>(sd.tree_n);
     PathDev pd{beta_.as<float4>(),  lpath_.as<float4>(), aov_a_.as<float4>(),
-               aov_n_.as<float4>(), ray_ff_.as<float4>(), opt_.record_samples ? sig_.as<uint32_t>() : nullptr};
+               aov_n_.as<float4>(), ray_ff_.as<float4>(), opt_.record_samples ? sig_.as<uint32_t>() : nullptr,
+               shadow_ff_.as<float4>()};
     FrameParams f{};
     f.cam = make_camera_basis(camera_, width_, height_);
     f.width = width_;
@@ -383,8 +388,8 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
     // default block: 256 threads over the 8-wide records (with the shared-memory stacks,
     // 0.3% faster than 128 on the 1M soup), 128 over the binary LBVH
     const int tb = opt_.trace_block ? static_cast<int>(opt_.trace_block) : (wide ? 256 : 128);
-    using ClosestFn = void (*)(SceneDev, const float4*, float4*, const int*, int, int*, uint32_t*, unsigned long long*);
-    using ShadowFn = void (*)(SceneDev, PathDev, const float4*, const int*, int, int*, uint32_t*, unsigned long long*);
+    using ClosestFn = void (*)(SceneDev, ClosestJob, const int*, int, int*, uint32_t*, unsigned long long*);
+    using ShadowFn = void (*)(SceneDev, ShadowJob, const int*, int, int*, uint32_t*, unsigned long long*);
     const int mode = wide ? (sd.refill < 32 ? k_mode_wide_refill : k_mode_wide)
                           : sd.refill < 32 ? k_mode_refill : (sd.tree_n > 0 ? k_mode_batch_tree : k_mode_batch);
     static const ClosestFn closest_fns[2][5] = {
@@ -414,6 +419,11 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
     const int grid_c = sm_count_ * std::max(occ_c, 1);
     const int grid_s = sm_count_ * std::max(occ_s, 1);
     const int grid_shade = sm_count_ * 8;
+    int occ_f = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, k_fixup<ClosestJob>, 256, wide_stack_smem_bytes<true>(256));
+    const int grid_fixup = sm_count_ * std::max(occ_f, 1);
+    const size_t smem_fc = wide ? wide_stack_smem_bytes<false>(256) : 0;
+    const size_t smem_fs = wide ? wide_stack_smem_bytes<true>(256) : 0;
     uint32_t* err = err_dev_.as<uint32_t>();
     unsigned long long* st = stats_dev_.as<unsigned long long>();
     const uint32_t px = width_ * height_;
@@ -437,19 +447,26 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
             int* c_shadow = cnt + D + (k - 1);
             int* f_cur = cnt + 2 * D + (k - 1);
             int* f_shadow = cnt + 3 * D + (k - 1);
+            const ClosestJob cjob{qcur, hits_.as<float4>(), ray_ff_.as<float4>(),
+                                  DeferList{defer_.as<int>(), cnt + 4 * D + (k - 1)}};
+            const ShadowJob sjob{shadow_.as<float4>(), pd, DeferList{defer_.as<int>(), cnt + 5 * D + (k - 1)}};
             R_TRY(QUASI_LAUNCH(prof_, "trace_closest", s,
-                               (kc<<<grid_c, tb, smem_c, s>>>(sd, qcur, hits_.as<float4>(), c_cur, cap, f_cur, err,
-                                                                 st))),
+                               (kc<<<grid_c, tb, smem_c, s>>>(sd, cjob, c_cur, cap, f_cur, err, st))),
                   "trace_closest");
+            R_TRY(QUASI_LAUNCH(prof_, "fixup_closest", s,
+                               (k_fixup<ClosestJob><<<grid_fixup, 256, smem_fc, s>>>(sd, cjob, cnt + 6 * D + (k - 1), err))),
+                  "fixup_closest");
             R_TRY(QUASI_LAUNCH(prof_, "shade", s,
                                (k_shade<<<grid_shade, 256, 0, s>>>(f, sd, pd, k, qcur, hits_.as<float4>(), c_cur, cap, qnext,
                                                                   k < D ? c_next : nullptr, shadow_.as<float4>(),
                                                                   c_shadow))),
                   "shade");
             R_TRY(QUASI_LAUNCH(prof_, "trace_shadow", s,
-                               (ks<<<grid_s, tb, smem_s, s>>>(sd, pd, shadow_.as<float4>(), c_shadow, cap, f_shadow,
-                                                                 err, st))),
+                               (ks<<<grid_s, tb, smem_s, s>>>(sd, sjob, c_shadow, cap, f_shadow, err, st))),
                   "trace_shadow");
+            R_TRY(QUASI_LAUNCH(prof_, "fixup_shadow", s,
+                               (k_fixup<ShadowJob><<<grid_fixup, 256, smem_fs, s>>>(sd, sjob, cnt + 7 * D + (k - 1), err))),
+                  "fixup_shadow");
         }
         R_TRY(QUASI_LAUNCH(prof_, "accumulate", s,
                            (k_accumulate<<<ceil_div(px, 256), 256, 0, s>>>(
@@ -511,7 +528,8 @@ int Renderer::render_megakernel(cudaStream_t s, uint32_t spp) {
     const SceneDev sd = Renderer_scene_dev(bvh_.view(), tri_in_, albedo_, emission_, emitters_, n_tris_, n_emit_,
                                            opt_.bvh_width);
     PathDev pd{beta_.as<float4>(),  lpath_.as<float4>(), aov_a_.as<float4>(),
-               aov_n_.as<float4>(), ray_ff_.as<float4>(), opt_.record_samples ? sig_.as<uint32_t>() : nullptr};
+               aov_n_.as<float4>(), ray_ff_.as<float4>(), opt_.record_samples ? sig_.as<uint32_t>() : nullptr,
+               shadow_ff_.as<float4>()};
     FrameParams f = frame_params(spp, slots, tiles_x);
     int occ = 0;
     auto kern = opt_.collect_stats ? k_megakernel<true> : k_megakernel<false>;
@@ -687,13 +705,14 @@ int Renderer::stats(Q_cuda_stats* out) {
         last_stats_ = st;
     } else if (stats_pending_) {
         const uint32_t D = opt_.max_depth;
-        const uint32_t per_wave = 4 * D;
+        const uint32_t per_wave = k_counters_per_bounce * D;
         const uint32_t waves = per_wave ? counters_used_ / per_wave : 0;
         for (uint32_t w = 0; w < waves; ++w) {
             const int* c = counters_host_ + w * per_wave;
             st.camera_rays += static_cast<uint64_t>(c[0]);
             for (uint32_t k = 1; k < D; ++k) st.extension_rays += static_cast<uint64_t>(c[k]);
             for (uint32_t k = 0; k < D; ++k) st.shadow_rays += static_cast<uint64_t>(c[D + k]);
+            for (uint32_t k = 0; k < 2 * D; ++k) st.redecided_rays += static_cast<uint64_t>(c[4 * D + k]);
         }
         if (opt_.collect_stats) {
             st.node_visits = stats_host_[0];

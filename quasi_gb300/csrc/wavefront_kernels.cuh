@@ -6,16 +6,21 @@
 //   for bounce k = 1..D:
 //     k_trace_closest persistent, warp-fetched closest-hit traversal of the queue (FP32),
 //                     over the 8-wide records (wide.cuh) or the binary LBVH nodes
+//     k_fixup         re-traces the rays the trace kernel could not decide for certain,
+//                     with exact (double-float) re-decisions (robust.cuh)
 //     k_shade         emission (k == 1), AOVs (k == 1), light sample -> shadow queue,
 //                     cosine-weighted continuation -> next ray queue; both queues are
 //                     compacted with one atomic per warp (ballot + popc)
 //     k_trace_shadow  persistent any-hit traversal (FP32); unoccluded rays add their
 //                     contribution to the owning path's radiance
+//     k_fixup         the same for the shadow rays
 //   k_accumulate      per pixel, Kahan-adds the wave's samples in sample order
 // Paths are addressed by a stable id (sample-in-wave * slots + tile-ordered pixel slot); a
 // path has at most one ray in each queue, so no two threads ever update the same path.
 //
-// Precision: traversal decides which triangle a ray hits in FP32. The path geometry (ray
+// Precision: traversal tests triangles in FP32 with a rigorous error bound per test; the
+// few rays that meet a candidate the bound cannot decide are re-traced with double-float
+// decisions, so every hit decision agrees with exact arithmetic. The path geometry (ray
 // origins and directions, the hit point, the light sample and the shading frame) is
 // carried in double-float (ffmath.cuh): each vertex re-intersects the hit triangle's plane
 // with the double-float ray, so a path's radiance matches the FP64 oracle to ~1e-7 even
@@ -23,6 +28,8 @@
 #pragma once
 
 #include "path.cuh"
+
+#include <type_traits>
 
 namespace quasi {
 
@@ -51,14 +58,13 @@ constexpr int trace_min_blocks(int mode) { return mode >= k_mode_wide ? QUASI_WI
 
 // Persistent closest-hit traversal.
 template <bool STATS, int MODE>
-__global__ void __launch_bounds__(256, trace_min_blocks(MODE)) k_trace_closest(SceneDev s, const float4* __restrict__ q,
-                                                       float4* __restrict__ hits, const int* __restrict__ count,
-                                                       int capacity, int* __restrict__ fetch,
-                                                       uint32_t* __restrict__ err, unsigned long long* __restrict__ stats) {
+__global__ void __launch_bounds__(256, trace_min_blocks(MODE)) k_trace_closest(SceneDev s, ClosestJob job,
+                                                       const int* __restrict__ count, int capacity,
+                                                       int* __restrict__ fetch, uint32_t* __restrict__ err,
+                                                       unsigned long long* __restrict__ stats) {
     const int n = min(*count, capacity);
     uint32_t e = 0;
     TraceCounters c;
-    ClosestJob job{q, hits};
     if (MODE == k_mode_wide)
         trace_batches_wide<false, STATS>(job, s.wide, s.tris, s.n_tris, n, fetch, e, c);
     else if (MODE == k_mode_wide_refill)
@@ -75,14 +81,13 @@ __global__ void __launch_bounds__(256, trace_min_blocks(MODE)) k_trace_closest(S
 
 // Persistent any-hit traversal of the shadow queue.
 template <bool STATS, int MODE>
-__global__ void __launch_bounds__(256, trace_min_blocks(MODE)) k_trace_shadow(SceneDev s, PathDev p, const float4* __restrict__ sq,
+__global__ void __launch_bounds__(256, trace_min_blocks(MODE)) k_trace_shadow(SceneDev s, ShadowJob job,
                                                       const int* __restrict__ count, int capacity,
                                                       int* __restrict__ fetch, uint32_t* __restrict__ err,
                                                       unsigned long long* __restrict__ stats) {
     const int n = min(*count, capacity);
     uint32_t e = 0;
     TraceCounters c;
-    ShadowJob job{sq, p};
     if (MODE == k_mode_wide)
         trace_batches_wide<true, STATS>(job, s.wide, s.tris, s.n_tris, n, fetch, e, c);
     else if (MODE == k_mode_wide_refill)
@@ -97,6 +102,32 @@ __global__ void __launch_bounds__(256, trace_min_blocks(MODE)) k_trace_shadow(Sc
     flush_counters<STATS>(c, stats + 2);
 }
 
+// Re-traces the rays a closest-hit or shadow trace kernel deferred (an undecided candidate:
+// robust.cuh) over the 8-wide records with per-lane refill, re-deciding undecided candidates
+// exactly, and stores their results. The list length is read on the device, so the launch
+// needs no host synchronisation. Launched like the trace kernels (shared-memory stacks).
+template <class Job>
+__global__ void __launch_bounds__(256, 2) k_fixup(SceneDev s, Job job, int* __restrict__ fetch,
+                                                                     uint32_t* __restrict__ err) {
+    constexpr bool any = std::is_same<Job, ShadowJob>::value;
+    uint32_t e = 0;
+    TraceCounters c;
+    FixupJob<Job> fj{job, job.deferred.list};
+    const int n = *job.deferred.count;
+    if (s.wide)
+        trace_wide_refill<any, false, FixupJob<Job>, true>(fj, s.wide, s.tris, s.n_tris, n, k_wide_refill_lanes, fetch,
+                                                           e, c, s.tri_in);
+    else
+        trace_fixups<any>(job, s.nodes, s.tris, s.tri_in, s.n_tris, job.deferred.list, n, fetch, e);
+    if (e) atomicOr(err, e);
+}
+
+// Per-wave frame counters, k_counters_per_bounce per bounce: [0, D) closest-hit queue
+// lengths, [D, 2D) shadow queue lengths, [2D, 3D) and [3D, 4D) their trace fetch counters,
+// [4D, 5D) and [5D, 6D) the rays each deferred to the fixup kernels, [6D, 8D) the fixup
+// kernels' fetch counters.
+constexpr uint32_t k_counters_per_bounce = 8;
+
 // Adds the frame's queue lengths (rays traced) to the cumulative counter stats[4]; one
 // warp, so the timed loop needs no host synchronisation to know how many rays it traced.
 __global__ void k_tally(const int* __restrict__ counters, uint32_t waves, uint32_t depth,
@@ -104,7 +135,7 @@ __global__ void k_tally(const int* __restrict__ counters, uint32_t waves, uint32
     unsigned long long sum = 0;
     for (uint32_t i = threadIdx.x; i < waves * 2 * depth; i += 32) {
         const uint32_t w = i / (2 * depth), k = i - w * 2 * depth;
-        sum += static_cast<unsigned long long>(max(counters[w * 4 * depth + k], 0));
+        sum += static_cast<unsigned long long>(max(counters[w * k_counters_per_bounce * depth + k], 0));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);

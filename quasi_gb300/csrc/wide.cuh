@@ -30,10 +30,15 @@
 //                  (code 3 = an empty slot: lo planes 255, hi planes 0, no triangles)
 //
 // Closest hit is the smallest t, and an exact tie goes to the smaller original index, as in
-// the binary traversal (trace.cuh), so both return the same triangle.
+// the binary traversal (trace.cuh), so both return the same triangle. Child boxes are padded
+// by the scene's Delta (scene_box_pad) before quantisation, and triangle tests classify
+// their candidates (robust.cuh): a ray that meets an undecided candidate ends with
+// k_prim_flagged and is re-traced exactly by the fixup kernel.
 #pragma once
 
 #include "trace.cuh"
+
+#include <type_traits>
 
 namespace quasi {
 
@@ -179,44 +184,26 @@ __device__ __forceinline__ float fmin3(float a, float b, float c) {
     return r;
 }
 
-// Tests the triangles of one leaf; returns true when an any-hit query is done.
-template <bool ANY, bool STATS>
-__device__ __forceinline__ bool wide_leaf(const float4* __restrict__ tris, const RayInv& r, int ref, float tmax,
-                                          int exclude, float& best_t, int& best, float& bu, float& bv,
-                                          TraceCounters& cnt) {
-    const uint32_t x = static_cast<uint32_t>(~ref);
-    const uint32_t pos = x >> 2;
-    // With one-triangle leaves (k_wide_leaf_max = 1) a leaf that passed its box test holds
-    // exactly one triangle (empty slots never pass), and the loop is a single test: 1.8%
-    // faster on the 1M soup than decoding the count.
-    const uint32_t count = k_wide_leaf_max == 1 ? 1u : ((x & 3u) + 1u) & 3u;
-    for (uint32_t j = 0; j < count; ++j) {
-        if (STATS) ++cnt.tris;
-        const float4* t = tris + 3ull * (pos + j);
-        const float4 a = __ldg(t), e1 = __ldg(t + 1), e2 = __ldg(t + 2);
-        const int orig = __float_as_int(a.w);
-        float u, v;
-        const float th = tri_t(r, a, e1, e2, u, v);
-        if (orig != exclude && (th < best_t || (th == best_t && orig < best && th < tmax))) {
-            best_t = th;
-            best = orig;
-            bu = u;
-            bv = v;
-            if (ANY) return true;
-        }
-    }
-    return false;
+// Tests the triangle of one leaf (one-triangle leaves: a leaf that passed its box test
+// holds exactly one triangle, empty slots never pass); returns true when the traversal ends
+// (an any-hit query answered, or an undecided candidate flagged the ray).
+// ROBUST: undecided candidates are re-decided exactly (tri_in: original-order vertices, xr:
+// the ray's exact geometry) instead of ending the traversal.
+template <bool ANY, bool STATS, bool ROBUST = false, class X = ExactNone>
+__device__ __forceinline__ bool wide_leaf(const float4* __restrict__ tris, const RayInv& r, int ref, int exclude,
+                                          HitBest& b, TraceCounters& cnt, const float4* __restrict__ tri_in = nullptr,
+                                          const X& xr = X{}) {
+    static_assert(k_wide_leaf_max == 1, "wide_leaf tests one triangle per leaf");
+    if (STATS) ++cnt.tris;
+    return leaf_test<ANY, ROBUST>(tris, tri_in, xr, r, static_cast<uint32_t>(~ref) >> 2, exclude, b);
 }
 
 // Traversal state of one ray over the 8-wide records (the stack lives beside it).
 struct WideRay {
     RayInv r;
     uint32_t oct;   // direction octant: bit a set where component a is negative
-    float tmax;
     int exclude;
-    float best_t;
-    int best;       // original index of the closest hit so far, or -1
-    float bu, bv;
+    HitBest b;      // closest hit so far (prim k_prim_flagged: undecided, re-trace exactly)
     int node;       // record to visit next, or k_wide_done
     int sp;
     uint32_t budget;
@@ -226,22 +213,21 @@ __device__ __forceinline__ void wide_begin(WideRay& q, float3 o, float3 d, float
     q.r = make_ray(o, d);
     // octant from the reciprocals, which carry the sign of a zero component (-0 -> -1e20)
     q.oct = (q.r.inv.x < 0.0f ? 1u : 0u) | (q.r.inv.y < 0.0f ? 2u : 0u) | (q.r.inv.z < 0.0f ? 4u : 0u);
-    q.tmax = tmax;
     q.exclude = exclude;
-    q.best_t = tmax;
-    q.best = -1;
-    q.bu = q.bv = 0.0f;
+    q.b = hit_begin(tmax);
     q.node = n_tris == 0 ? k_wide_done : 0;
     q.sp = 0;
     q.budget = 2u * n_tris + 64u;
 }
 
-// Pops the nearest stacked entry still closer than the best hit, or k_wide_done.
+// Pops the nearest stacked entry entered before the closest hit's t plus its error bound,
+// or k_wide_done.
 template <class Stack>
 __device__ __forceinline__ int wide_pop(WideRay& q, const Stack& stack) {
+    const float tcull = q.b.t + q.b.dt;
     while (q.sp > 0) {
         const int2 e = stack.get(--q.sp);
-        if (__int_as_float(e.y) < q.best_t) return e.x;
+        if (__int_as_float(e.y) < tcull) return e.x;
     }
     return k_wide_done;
 }
@@ -252,9 +238,10 @@ __device__ __forceinline__ int wide_pop(WideRay& q, const Stack& stack) {
 // visit and stacking the other leaves (each loop turn then costs one triangle test, not the
 // busiest lane's count) was measured 7% slower on the 1M soup: the extra stack traffic and
 // loop turns cost more than the divergence they remove.
-template <bool ANY, bool STATS, class Stack>
+template <bool ANY, bool STATS, class Stack, bool ROBUST = false, class X = ExactNone>
 __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, const float4* __restrict__ tris,
-                                           WideRay& q, Stack& stack, uint32_t& err, TraceCounters& cnt) {
+                                           WideRay& q, Stack& stack, uint32_t& err, TraceCounters& cnt,
+                                           const float4* __restrict__ tri_in = nullptr, const X& xr = X{}) {
     if (q.node == k_wide_done) return true;
     if (--q.budget == 0u) {
         err |= k_deverr_traversal;
@@ -289,6 +276,7 @@ __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, cons
     // any-hit rays: the internal child whose box covers the longest stretch of the segment
     float best_ov = -1.0f;
     uint32_t best_slot = 0;
+    const float tcull = q.b.t + q.b.dt;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         const uint32_t nxw = k < 4 ? nx0 : nx1, fxw = k < 4 ? fx0 : fx1;
@@ -306,7 +294,7 @@ __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, cons
         float tnz, tfz;
         f2_unpack(f2_fma(f2_sub(f2_pack(byte_f23(nzw, b), byte_f23(fzw, b)), c23), azz, bzz), tnz, tfz);
         const float tnear = fmax3(tnx, tny, fmaxf(tnz, 0.0f));
-        const float tfar = fmin3(tfx, tfy, fminf(tfz, q.best_t));
+        const float tfar = fmin3(tfx, tfy, fminf(tfz, tcull));
         tn[k] = tnear;
         const bool h = tnear <= tfar * k_box_pad;
         hit |= (h ? 1u : 0u) << k;
@@ -327,7 +315,7 @@ __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, cons
     while (lm) {
         const uint32_t s = __ffs(lm) - 1;
         lm &= lm - 1u;
-        if (wide_leaf<ANY, STATS>(tris, r, sel8(refs, s), q.tmax, q.exclude, q.best_t, q.best, q.bu, q.bv, cnt)) {
+        if (wide_leaf<ANY, STATS, ROBUST>(tris, r, sel8(refs, s), q.exclude, q.b, cnt, tri_in, xr)) {
             q.node = k_wide_done;
             return true;
         }
@@ -359,7 +347,7 @@ __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, cons
         im &= im - 1u;
         const uint32_t s = p ^ q.oct;
         const float t = sel8(tn, s);
-        if (t >= q.best_t) continue;
+        if (t >= q.b.t + q.b.dt) continue;
         const int ref = sel8(refs, s);
         if (im) {
             if (q.sp >= k_wide_stack) {
@@ -377,22 +365,19 @@ __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, cons
     return next == k_wide_done;
 }
 
-// Whole-ray traversal of the 8-wide BVH; same contract as trace_bvh (trace.cuh):
-// ANY = true stops at the first hit with t in (0, tmax). Returns the original index of the
-// hit triangle (or -1), its distance in t_out and its barycentrics in bu, bv.
+// Whole-ray traversal of the 8-wide BVH (fast mode); same contract as trace_bvh
+// (trace.cuh): ANY = true stops at the first hit with t in (0, tmax); prim is the original
+// index of the hit triangle, -1, or k_prim_flagged when an undecided candidate was met.
 template <bool ANY, bool STATS>
-__device__ __forceinline__ int trace_wide(const float4* __restrict__ wide, const float4* __restrict__ tris,
-                                          uint32_t n_tris, const RayInv& r, float tmax, int exclude, float& t_out,
-                                          float& bu, float& bv, uint32_t& err, TraceCounters& cnt) {
+__device__ __forceinline__ TraceResult trace_wide(const float4* __restrict__ wide, const float4* __restrict__ tris,
+                                                  uint32_t n_tris, float3 o, float3 d, float tmax, int exclude,
+                                                  uint32_t& err, TraceCounters& cnt) {
     WideRay q;
-    wide_begin(q, r.o, r.d, tmax, exclude, n_tris);
+    wide_begin(q, o, d, tmax, exclude, n_tris);
     WideStack<0> stack;
     while (!wide_visit<ANY, STATS>(wide, tris, q, stack, err, cnt)) {
     }
-    t_out = q.best_t;
-    bu = q.bu;
-    bv = q.bv;
-    return q.best;
+    return trace_result(q.b);
 }
 
 // Warp-batch persistent traversal of a ray queue over the 8-wide records: a warp takes 32
@@ -413,11 +398,7 @@ __device__ __forceinline__ void trace_batches_wide(Job& job, const float4* __res
             float tmax;
             int exclude;
             job.load(i, o, d, tmax, exclude);
-            TraceState s;
-            s.r = make_ray(o, d);
-            s.tmax = tmax;
-            s.best = trace_wide<ANY, STATS>(wide, tris, n_tris, s.r, tmax, exclude, s.best_t, s.bu, s.bv, err, cnt);
-            job.store(i, s);
+            finish_ray(job, i, trace_wide<ANY, STATS>(wide, tris, n_tris, o, d, tmax, exclude, err, cnt));
         }
     }
 }
@@ -427,14 +408,19 @@ __device__ __forceinline__ void trace_batches_wide(Job& job, const float4* __res
 // their own rays (refill = 32 waits for the whole warp). Job as in trace_batches. Every
 // lane of the warp must call this (it uses full-warp votes), and the block must be launched
 // with wide_stack_smem_bytes<ANY>(blockDim.x) of dynamic shared memory.
-template <bool ANY, bool STATS, class Job>
+// ROBUST (the fixup kernels): undecided candidates are re-decided inline from the job's
+// exact(i) geometry and the original-order vertices tri_in, and every ray is stored.
+template <bool ANY, bool STATS, class Job, bool ROBUST = false>
 __device__ __forceinline__ void trace_wide_refill(Job& job, const float4* __restrict__ wide,
                                                   const float4* __restrict__ tris, uint32_t n_tris, int n, int refill,
-                                                  int* __restrict__ fetch, uint32_t& err, TraceCounters& cnt) {
+                                                  int* __restrict__ fetch, uint32_t& err, TraceCounters& cnt,
+                                                  const float4* __restrict__ tri_in = nullptr) {
     const int lane = threadIdx.x & 31;
     WideRay q;
     WideStack<wide_smem_stack<ANY>()> stack;
     stack.slot = wide_stack_slot<ANY>();
+    using X = typename std::conditional<ROBUST, ExactPtr, ExactNone>::type;
+    X xr{};
     bool active = false, exhausted = false;
     int idx = 0;
     while (true) {
@@ -452,6 +438,7 @@ __device__ __forceinline__ void trace_wide_refill(Job& job, const float4* __rest
                     float tmax;
                     int exclude;
                     job.load(idx, o, d, tmax, exclude);
+                    if constexpr (ROBUST) xr = job.exact(idx);
                     wide_begin(q, o, d, tmax, exclude, n_tris);
                     active = true;
                 }
@@ -462,22 +449,32 @@ __device__ __forceinline__ void trace_wide_refill(Job& job, const float4* __rest
         if (active) {
 #pragma unroll 1
             for (int i = 0; i < k_wide_visits_per_check; ++i) {
-                done = wide_visit<ANY, STATS>(wide, tris, q, stack, err, cnt);
+                done = wide_visit<ANY, STATS, WideStack<wide_smem_stack<ANY>()>, ROBUST>(wide, tris, q, stack, err, cnt,
+                                                                                       tri_in, xr);
                 if (done) break;
             }
         }
         if (done) {
-            TraceState s;
-            s.r = q.r;
-            s.tmax = q.tmax;
-            s.best_t = q.best_t;
-            s.best = q.best;
-            s.bu = q.bu;
-            s.bv = q.bv;
-            job.store(idx, s);
+            if constexpr (ROBUST)
+                job.store(idx, trace_result(q.b));
+            else
+                finish_ray(job, idx, trace_result(q.b));
             active = false;
         }
     }
 }
+
+// A job over the entries of a fixup list: entry k is ray list[k] of the underlying job.
+template <class Job>
+struct FixupJob {
+    Job job;
+    const int* __restrict__ list;
+    __device__ __forceinline__ void load(int k, float3& o, float3& d, float& tmax, int& exclude) const {
+        job.load(list[k], o, d, tmax, exclude);
+    }
+    __device__ __forceinline__ void store(int k, const TraceResult& r) const { job.store(list[k], r); }
+    __device__ __forceinline__ ExactPtr exact(int k) const { return job.exact(list[k]); }
+    __device__ __forceinline__ int pid(int k) const { return job.pid(list[k]); }
+};
 
 }  // namespace quasi

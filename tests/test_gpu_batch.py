@@ -86,7 +86,7 @@ def _check_batch(host, scenes, single, **opts):
 def test_batch_equals_single_scene_renders(scenes, single):
     host = q.PluginHost()
     st = _check_batch(host, scenes, single)
-    assert st.scenes == len(scenes) and st.waves == 1 and st.kernels_per_frame == 2 + 3 * DEPTH + 2
+    assert st.scenes == len(scenes) and st.waves == 1 and st.kernels_per_frame == 2 + 5 * DEPTH + 2
     host.destroy()
 
 
