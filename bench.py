@@ -144,28 +144,6 @@ def cpu_sample(scene, precision: int = 32, target_s: float = 12.0, seed: int = 0
     return rays / dt / 1e6, threads, desc
 
 
-def batch_scene_list(lib, count: int, seed0: int, tris: tuple[float, float], sizes: tuple[int, ...],
-                     spps: tuple[int, ...]) -> list:
-    """Soup scenes with seeds seed0 .. seed0 + count - 1; each scene's triangle count
-    (log-uniform in `tris`), square resolution and spp are drawn from numpy's default_rng
-    seeded with the scene seed."""
-    import math
-
-    import numpy as np
-
-    import quasi_gb300 as q
-
-    out = []
-    for i in range(count):
-        seed = seed0 + i
-        rng = np.random.default_rng(seed)
-        n = int(round(math.exp(rng.uniform(math.log(tris[0]), math.log(tris[1])))))
-        res = int(rng.choice(sizes))
-        spp = int(rng.choice(spps))
-        out.append((q.make_scene(f"soup:n={n},seed={seed}", lib), res, res, spp))
-    return out
-
-
 def bench_batch(host, stream, flush, steps: int, warmup: int, budget_ms: float, small: bool = False) -> dict:
     """Batching workload: 64 soup scenes (seeds 1..64, 1e3..5e5 triangles, 64^2..1024^2 pixels,
     4/16/64 spp, depth 6) rendered as one batch (one graph launch per frame, autotuned),
@@ -175,12 +153,13 @@ def bench_batch(host, stream, flush, steps: int, warmup: int, budget_ms: float, 
     import torch
 
     import quasi_gb300 as q
+    from quasi_gb300 import workloads
 
     if small:
-        scenes = batch_scene_list(host.lib, 64, 1, (1e3, 5e4), (64, 128), (4,))
+        scenes = workloads.BATCH_64_SMALL.scenes(host.lib)
         label = "64 soup scenes, seeds 1..64, log-uniform 1e3..5e4 triangles, 64^2..128^2 pixels, 4 spp, depth 6"
     else:
-        scenes = batch_scene_list(host.lib, 64, 1, (1e3, 5e5), (64, 128, 256, 512, 1024), (4, 16, 64))
+        scenes = workloads.BATCH_64.scenes(host.lib)
         label = "64 soup scenes, seeds 1..64, log-uniform 1e3..5e5 triangles, 64^2..1024^2 pixels, spp 4/16/64, depth 6"
     depth = 6
     res = {"workload": label + ", BVHs built once",
@@ -255,6 +234,7 @@ def bench_diff(stream, steps: int, fit_steps: int) -> dict:
 
     import quasi_gb300 as q
     from quasi_gb300 import autograd as qa
+    from quasi_gb300 import workloads
 
     out = {}
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
@@ -297,7 +277,7 @@ def bench_diff(stream, steps: int, fit_steps: int) -> dict:
                           "rays_forward": r_f / steps, "rays_adjoint": r_b / steps}
         # (b) batched differentiation
         lib = q.load_library()
-        scenes = batch_scene_list(lib, 32, 101, (2e3, 1e5), (128, 256, 512), (8,))
+        scenes = workloads.BATCH_DIFF_32.scenes(lib)
         bhost, batch = qa.make_batch(scenes, max_depth=4, seed=0)
         gt = torch.tensor(np.concatenate([sc.albedo for sc, *_ in scenes]), device="cuda")
         em = torch.tensor(np.concatenate([sc.emission for sc, *_ in scenes]), device="cuda")
@@ -312,7 +292,7 @@ def bench_diff(stream, steps: int, fit_steps: int) -> dict:
         seen = (a0.grad.abs().sum(dim=1) > 0)
         st0 = batch.stats()
         ev[0].record()
-        fitted, losses = qa.fit_albedo(batch, target, init, em, steps=fit_steps, lr=0.01)
+        fitted, losses = qa.fit_albedo(batch, None, init, em, steps=fit_steps, lr=0.01, target_albedo=gt, seed0=1)
         ev[1].record()
         torch.cuda.synchronize()
         st1 = batch.stats()
@@ -325,12 +305,13 @@ def bench_diff(stream, steps: int, fit_steps: int) -> dict:
 
         out["batched_fit"] = {
             "workload": "32 soup scenes, seeds 101..132, log-uniform 2e3..1e5 triangles, 128^2..512^2 pixels, "
-                        "8 spp, depth 4, Adam lr 0.01",
+                        "8 spp, depth 4, Adam lr 0.01; every step re-seeded, its target rendered from the true "
+                        "albedo with the step's seed (rays of both forwards and the adjoint counted)",
             "steps": fit_steps, "tri_total": int(gt.shape[0]), "px_total": int(st1.px_total),
             "mrays_s_forward_plus_adjoint": rays / ms / 1e3, "ms_per_step": ms / fit_steps,
             "rmse_init_all": rmse(init), "rmse_final_all": rmse(fitted),
             "triangles_seen": int(seen.sum()), "rmse_init_seen": rmse(init, seen), "rmse_final_seen": rmse(fitted, seen),
-            "loss_first": losses[0], "loss_last": losses[-1], "graph_launches_per_step": 2}
+            "loss_first": losses[0], "loss_last": losses[-1], "graph_launches_per_step": 3}
         batch.destroy()
         bhost.destroy()
     return out

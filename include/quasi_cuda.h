@@ -409,6 +409,11 @@ Q_CUDA_EXPORT int Q_cuda_batch_get_options(Q_cuda_batch* batch, Q_cuda_batch_opt
 Q_CUDA_EXPORT int Q_cuda_batch_render(Q_cuda_batch* batch, void* stream);
 /* Clears the accumulation of every scene (the next frame starts at sample 0). */
 Q_CUDA_EXPORT int Q_cuda_batch_reset(Q_cuda_batch* batch);
+/* Changes the RNG seed of every scene and clears the accumulation, on `stream` (NULL = the
+ * plugin's stream): a device-side update of the scene table, so the captured frame and
+ * adjoint graphs stay valid. An optimisation loop calls it once per step to draw new paths
+ * (the target and the rendered image of a step then share the seed). */
+Q_CUDA_EXPORT int Q_cuda_batch_set_seed(Q_cuda_batch* batch, uint32_t seed, void* stream);
 /* Waits for the batch's work; returns QUASI_ERR_STACK / QUASI_ERR_TIMEOUT for device errors. */
 Q_CUDA_EXPORT int Q_cuda_batch_synchronize(Q_cuda_batch* batch);
 Q_CUDA_EXPORT int Q_cuda_batch_get_stats(Q_cuda_batch* batch, Q_cuda_batch_stats* stats);

@@ -184,6 +184,7 @@ CUDA_SYMBOLS = {
     "Q_cuda_batch_get_options": (C.c_int, [C.c_void_p, C.POINTER(Q_cuda_batch_options)]),
     "Q_cuda_batch_render": (C.c_int, [C.c_void_p, C.c_void_p]),
     "Q_cuda_batch_reset": (C.c_int, [C.c_void_p]),
+    "Q_cuda_batch_set_seed": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),
     "Q_cuda_batch_synchronize": (C.c_int, [C.c_void_p]),
     "Q_cuda_batch_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Q_cuda_batch_stats)]),
     "Q_cuda_batch_readback": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),

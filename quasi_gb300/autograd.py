@@ -121,19 +121,29 @@ def render_batch(albedo: torch.Tensor, emission: torch.Tensor, batch: Batch) -> 
     return BatchRenderFunction.apply(albedo, emission, batch, int(batch.stats().px_total))
 
 
-def fit_albedo(batch: Batch, target: torch.Tensor, albedo0: torch.Tensor, emission: torch.Tensor, steps: int = 100,
-               lr: float = 0.01) -> tuple[torch.Tensor, list[float]]:
+def fit_albedo(batch: Batch, target: torch.Tensor | None, albedo0: torch.Tensor, emission: torch.Tensor,
+               steps: int = 100, lr: float = 0.01, target_albedo: torch.Tensor | None = None,
+               seed0: int = 0) -> tuple[torch.Tensor, list[float]]:
     """Adam on the per-triangle albedo of every scene of the batch against target images
     (L2 loss, mean over pixels and channels); albedo is kept in [0, 1] after each step.
     Adam's eps is 1e-15: the gradients of these mostly dark images are ~1e-10, far below the
     usual 1e-8, which would otherwise shrink every step by that ratio.
+    With target_albedo, every step k draws new paths: the batch is re-seeded with seed0 + k
+    and the target is rendered from target_albedo with that seed before the fitted image, so
+    both see the same paths (target is then unused). Otherwise every step renders the same
+    samples against the fixed target.
     Returns the fitted albedo and the loss of every step."""
     albedo = albedo0.detach().clone().requires_grad_(True)
     opt = torch.optim.Adam([albedo], lr=lr, eps=1e-15)
     px = int(batch.stats().px_total)
+    stream = torch_stream_handle()
     losses = []
-    for _ in range(steps):
+    for k in range(steps):
         opt.zero_grad(set_to_none=True)
+        if target_albedo is not None:
+            batch.set_seed(seed0 + k, stream)
+            with torch.no_grad():
+                target = BatchRenderFunction.apply(target_albedo, emission, batch, px).clone()
         img = BatchRenderFunction.apply(albedo, emission, batch, px)
         loss = ((img - target) ** 2).mean()
         loss.backward()

@@ -224,8 +224,8 @@ int BatchRenderer::upload_table() {
 int BatchRenderer::plan(uint32_t spp_cap) {
     // per path slot: two ray queues (2 x 32), hit 16, shadow ray 48, beta, radiance and two
     // AOVs (4 x 16), double-float ray 48, (scene, local path) 8, exact shadow segment 48,
-    // fixup list entry 4
-    constexpr size_t bytes_per_path = 300;
+    // fixup list entry 8
+    constexpr size_t bytes_per_path = 304;
     uint32_t W = opt_.wave_paths ? opt_.wave_paths
                                  : static_cast<uint32_t>(wave_paths_fitting(k_default_wave_paths, bytes_per_path,
                                                                             size_t(wave_capacity_) * bytes_per_path));
@@ -281,7 +281,7 @@ int BatchRenderer::ensure_buffers() {
         B_TRY(pn_.reserve(sizeof(float4) * paths), "aov");
         B_TRY(ray_ff_.reserve(sizeof(float4) * 3ull * paths), "ray_ff");
         B_TRY(shadow_ff_.reserve(sizeof(float4) * 3ull * paths), "shadow_ff");
-        B_TRY(defer_.reserve(sizeof(int) * paths), "defer");
+        B_TRY(defer_.reserve(sizeof(int2) * paths), "defer");
         B_TRY(meta_.reserve(sizeof(uint2) * paths), "meta");
         wave_capacity_ = paths;
         graphs_dirty_ = true;
@@ -346,9 +346,7 @@ int BatchRenderer::record_frame(cudaStream_t s, uint32_t& launches) {
     auto km = stats ? k_batch_megakernel<true> : k_batch_megakernel<false>;
     const int grid_c = grid_c_, grid_s = grid_s_, grid_m = grid_m_;
     const int grid_shade = sm * 8;
-    const int grid_fixup = grid_c;
-    auto kfc = wide ? k_batch_fixup<ClosestJob, true> : k_batch_fixup<ClosestJob, false>;
-    auto kfs = wide ? k_batch_fixup<ShadowJob, true> : k_batch_fixup<ShadowJob, false>;
+    const int grid_fixup = sm * 4;
     const int cap = static_cast<int>(wave_capacity_);
     for (size_t w = 0; w < waves_.size(); ++w) {
         const Wave& wv = waves_[w];
@@ -373,14 +371,15 @@ int BatchRenderer::record_frame(cudaStream_t s, uint32_t& launches) {
                 int* f_cur = cnt + 2 * D + (k - 1);
                 int* f_shadow = cnt + 3 * D + (k - 1);
                 const ClosestJob cjob{qcur, hits_.as<float4>(), ray_ff_.as<float4>(),
-                                      DeferList{defer_.as<int>(), cnt + 4 * D + (k - 1)}};
-                const ShadowJob sjob{shadow_.as<float4>(), pd, DeferList{defer_.as<int>(), cnt + 5 * D + (k - 1)}};
+                                      DeferList{defer_.as<int2>(), cnt + 4 * D + (k - 1)}};
+                const ShadowJob sjob{shadow_.as<float4>(), pd, DeferList{defer_.as<int2>(), cnt + 5 * D + (k - 1)}};
                 B_TRY(QUASI_LAUNCH(prof_, "batch_trace_closest", s,
                                    (kc<<<grid_c, tb, smem_c_, s>>>(table, meta, cjob, c_cur, cap, chunk, refill, f_cur, err,
                                                                    st))),
                       "batch_trace_closest");
                 B_TRY(QUASI_LAUNCH(prof_, "batch_fixup_closest", s,
-                                   (kfc<<<grid_fixup, tb, smem_c_, s>>>(table, meta, cjob, cnt + 6 * D + (k - 1), err))),
+                                   (k_batch_fixup<ClosestJob><<<grid_fixup, 128, 0, s>>>(table, meta, cjob,
+                                                                                        cnt + 6 * D + (k - 1), err))),
                       "batch_fixup_closest");
                 B_TRY(QUASI_LAUNCH(prof_, "batch_shade", s,
                                    (k_batch_shade<<<grid_shade, 256, 0, s>>>(table, meta, pd, k, qcur, hits_.as<float4>(),
@@ -392,7 +391,8 @@ int BatchRenderer::record_frame(cudaStream_t s, uint32_t& launches) {
                                                                    err, st))),
                       "batch_trace_shadow");
                 B_TRY(QUASI_LAUNCH(prof_, "batch_fixup_shadow", s,
-                                   (kfs<<<grid_s, tb, smem_s_, s>>>(table, meta, sjob, cnt + 7 * D + (k - 1), err))),
+                                   (k_batch_fixup<ShadowJob><<<grid_fixup, 128, 0, s>>>(table, meta, sjob,
+                                                                                       cnt + 7 * D + (k - 1), err))),
                       "batch_fixup_shadow");
             }
         }
@@ -521,6 +521,18 @@ int BatchRenderer::reset() {
                                                          static_cast<uint32_t>(scenes_.size())))),
           "batch_rewind");
     timed_ = false;
+    frames_since_reset_ = 0;
+    return QUASI_OK;
+}
+
+int BatchRenderer::set_seed(uint32_t seed, cudaStream_t stream) {
+    cudaStream_t s = pick(stream);
+    opt_.seed = seed;
+    for (DeviceBuffer* b : {&accum_, &comp_, &aov_a_, &aov_n_}) B_TRY(cudaMemsetAsync(b->ptr, 0, b->bytes, s), "memset");
+    B_TRY(QUASI_LAUNCH(prof_, "batch_reseed", s,
+                       (k_batch_reseed<<<1, 256, 0, s>>>(table_.as<BatchSceneDev>(),
+                                                         static_cast<uint32_t>(scenes_.size()), seed))),
+          "batch_reseed");
     frames_since_reset_ = 0;
     return QUASI_OK;
 }

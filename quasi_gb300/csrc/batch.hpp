@@ -29,6 +29,7 @@ public:
     Q_cuda_batch_options options() const { return opt_; }
     int render(cudaStream_t stream);
     int reset();
+    int set_seed(uint32_t seed, cudaStream_t stream);
     int synchronize();
     int stats(Q_cuda_batch_stats* out);
     int readback(uint32_t index, float* host_rgba);

@@ -105,10 +105,8 @@ __device__ __forceinline__ void trace_batches_multi(Job& job, const BatchSceneDe
                 int exclude;
                 job.load(i, o, d, tmax, exclude);
                 const RayInv r = make_ray(o, d, s.n_tris ? scene_box_pad(s.nodes) : 0.0f);
-                TraceResult res;
-                res.prim = trace_bvh<ANY, STATS>(s.nodes, s.tris, nullptr, s.n_tris, r, tmax, exclude, res.t, res.u,
-                                                 res.v, err, cnt);
-                finish_ray(job, i, res);
+                finish_ray(job, i, trace_result(trace_bvh<ANY, STATS>(s.nodes, s.tris, nullptr, s.n_tris, r, tmax,
+                                                                      exclude, err, cnt)));
             }
         }
     }
@@ -118,9 +116,7 @@ __device__ __forceinline__ void trace_batches_multi(Job& job, const BatchSceneDe
 // records: once `refill` lanes of a warp are idle they take the next rays with one atomic;
 // each lane traverses the records of its own ray's scene. Blocks are launched with
 // wide_stack_smem_bytes<ANY>(blockDim.x) of dynamic shared memory (the stacks' shared part).
-// ROBUST (the fixup kernel): undecided candidates are re-decided inline from job.exact(i)
-// and the scene's original-order vertices, and every ray is stored.
-template <bool ANY, bool STATS, class Job, bool ROBUST = false>
+template <bool ANY, bool STATS, class Job>
 __device__ __forceinline__ void trace_wide_refill_multi(Job& job, const BatchSceneDev* __restrict__ scenes,
                                                         const uint2* __restrict__ meta, int n, int refill,
                                                         int* __restrict__ fetch, uint32_t& err, TraceCounters& cnt) {
@@ -130,9 +126,6 @@ __device__ __forceinline__ void trace_wide_refill_multi(Job& job, const BatchSce
     stack.slot = wide_stack_slot<ANY>();
     const float4* wide = nullptr;
     const float4* tris = nullptr;
-    const float4* tri_in = nullptr;
-    using X = typename std::conditional<ROBUST, ExactPtr, ExactNone>::type;
-    X xr{};
     bool active = false, exhausted = false;
     int idx = 0;
     while (true) {
@@ -149,12 +142,10 @@ __device__ __forceinline__ void trace_wide_refill_multi(Job& job, const BatchSce
                     const SceneDev& s = scenes[meta[job.pid(idx)].x].s;
                     wide = s.wide;
                     tris = s.tris;
-                    tri_in = s.tri_in;
                     float3 o, d;
                     float tmax;
                     int exclude;
                     job.load(idx, o, d, tmax, exclude);
-                    if constexpr (ROBUST) xr = job.exact(idx);
                     wide_begin(q, o, d, tmax, exclude, s.n_tris);
                     active = true;
                 }
@@ -165,16 +156,12 @@ __device__ __forceinline__ void trace_wide_refill_multi(Job& job, const BatchSce
         if (active) {
 #pragma unroll 1
             for (int i = 0; i < k_wide_visits_per_check; ++i) {
-                done = wide_visit<ANY, STATS, WideStack<wide_smem_stack<ANY>()>, ROBUST>(wide, tris, q, stack, err, cnt,
-                                                                                       tri_in, xr);
+                done = wide_visit<ANY, STATS>(wide, tris, q, stack, err, cnt);
                 if (done) break;
             }
         }
         if (done) {
-            if constexpr (ROBUST)
-                job.store(idx, trace_result(q.b));
-            else
-                finish_ray(job, idx, trace_result(q.b));
+            finish_ray(job, idx, trace_result(q.b));
             active = false;
         }
     }
@@ -218,42 +205,43 @@ __global__ void __launch_bounds__(256, WIDE ? QUASI_WIDE_MIN_BLOCKS : 1) k_batch
     flush_counters<STATS>(c, stats + 2);
 }
 
-// Re-traces the rays a batch trace kernel deferred (robust.cuh) with exact re-decisions: over
-// the 8-wide records of each ray's scene with per-lane refill (WIDE, launched like the wide
-// trace kernels), else over the binary LBVHs, one ray per thread.
-template <class Job, bool WIDE>
-__global__ void __launch_bounds__(256, WIDE ? QUASI_WIDE_MIN_BLOCKS : 1) k_batch_fixup(
-    const BatchSceneDev* __restrict__ scenes, const uint2* __restrict__ meta, Job job, int* __restrict__ fetch,
-    uint32_t* __restrict__ err) {
+// Completes the rays a batch trace kernel deferred (robust.cuh) with each ray's scene:
+// re-decides its recorded candidate exactly against its certain result, or re-traces a ray
+// that met more than one over the scene's binary LBVH. One entry per thread.
+template <class Job>
+__global__ void __launch_bounds__(128) k_batch_fixup(const BatchSceneDev* __restrict__ scenes,
+                                                     const uint2* __restrict__ meta, Job job,
+                                                     int* __restrict__ fetch, uint32_t* __restrict__ err) {
     constexpr bool any = std::is_same<Job, ShadowJob>::value;
+    const int lane = threadIdx.x & 31;
     const int n = *job.deferred.count;
     uint32_t e = 0;
     TraceCounters cnt;
-    if constexpr (WIDE) {
-        FixupJob<Job> fj{job, job.deferred.list};
-        trace_wide_refill_multi<any, false, FixupJob<Job>, true>(fj, scenes, meta, n, k_wide_refill_lanes, fetch, e,
-                                                                 cnt);
-    } else {
-        const int lane = threadIdx.x & 31;
-        while (true) {
-            int base = 0;
-            if (lane == 0) base = atomicAdd(fetch, 32);
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (base >= n) break;
-            const int k = base + lane;
-            if (k < n) {
-                const int i = job.deferred.list[k];
-                const SceneDev& s = scenes[meta[job.pid(i)].x].s;
+    while (true) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(fetch, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const int k = base + lane;
+        if (k < n) {
+            const int2 en = job.deferred.list[k];
+            const int i = en.x;
+            const SceneDev& s = scenes[meta[job.pid(i)].x].s;
+            HitBest b;
+            if (en.y == k_undec_many) {
                 float3 o, d;
                 float tmax;
                 int exclude;
                 job.load(i, o, d, tmax, exclude);
                 const RayInv r = make_ray(o, d, s.n_tris ? scene_box_pad(s.nodes) : 0.0f);
-                TraceResult res;
-                res.prim = trace_bvh<any, false, false, true>(s.nodes, s.tris, s.tri_in, s.n_tris, r, tmax, exclude,
-                                                              res.t, res.u, res.v, e, cnt, job.exact(i));
-                job.store(i, res);
+                b = trace_bvh<any, false, false, true>(s.nodes, s.tris, s.tri_in, s.n_tris, r, tmax, exclude, e, cnt,
+                                                       job.exact(i));
+            } else {
+                b = job.partial(i);
+                redecide<any>(s.tri_in, job.exact(i), en.y, b);
             }
+            b.undec = k_undec_none;
+            job.store(i, trace_result(b));
         }
     }
     if (e) atomicOr(err, e);
@@ -444,6 +432,14 @@ __global__ void k_batch_advance(BatchSceneDev* __restrict__ scenes, uint32_t n, 
 // Clears the accumulation of a reset: sample bases back to 0.
 __global__ void k_batch_rewind(BatchSceneDev* __restrict__ scenes, uint32_t n) {
     for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) scenes[i].f.sample_base = 0;
+}
+
+// A new RNG seed for every scene, and sample bases back to 0.
+__global__ void k_batch_reseed(BatchSceneDev* __restrict__ scenes, uint32_t n, uint32_t seed) {
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        scenes[i].f.seed = seed;
+        scenes[i].f.sample_base = 0;
+    }
 }
 
 // Mean beauty image over pixels [px_begin, px_begin + px_count) of the batch image pool, as

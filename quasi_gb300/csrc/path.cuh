@@ -69,12 +69,12 @@ struct PathDev {
                         // (start, end - start in double-float), for exact re-decisions
 };
 
-// List of rays a fast trace kernel could not decide for certain (robust.cuh); the fixup
-// kernel re-traces them with exact re-decisions.
+// Rays a fast trace kernel could not decide for certain (robust.cuh): entries (ray index,
+// undecided candidate) for the fixup kernel.
 struct DeferList {
-    int* list;
+    int2* list;
     int* count;
-    __device__ __forceinline__ void push(int i) const { list[atomicAdd(count, 1)] = i; }
+    __device__ __forceinline__ void push(int i, int undec) const { list[atomicAdd(count, 1)] = make_int2(i, undec); }
 };
 
 // Pixel slots are ordered in 8x4 tiles so a warp's camera rays cover a compact patch.
@@ -159,8 +159,9 @@ __device__ __forceinline__ bool begin_path(const FrameParams& f, const PathDev& 
 }
 
 // Closest-hit queue: ray i is q[2i] = (origin, path id), q[2i+1] = (direction, excluded
-// triangle); the result is hits[i] = (t, triangle or -1, u, v). The exact ray of path pid is
-// ray_ff[3 pid] (the path's double-float segment).
+// triangle); the result is hits[i] = (t, triangle or -1, 0, 0). The exact ray of path pid is
+// ray_ff[3 pid] (the path's double-float segment). A deferred ray leaves its certain result
+// in hits[i] for the fixup kernel.
 struct ClosestJob {
     const float4* __restrict__ q;
     float4* __restrict__ hits;
@@ -168,7 +169,19 @@ struct ClosestJob {
     DeferList deferred;
     __device__ __forceinline__ int pid(int i) const { return __float_as_int(q[2 * i].w); }
     __device__ __forceinline__ ExactPtr exact(int i) const { return ExactPtr{ray_ff + 3ull * pid(i)}; }
-    __device__ __forceinline__ void defer(int i) const { deferred.push(i); }
+    __device__ __forceinline__ void defer(int i, const TraceResult& r) const {
+        store(i, r);
+        deferred.push(i, r.undec);
+    }
+    __device__ __forceinline__ HitBest partial(int i) const {
+        const float4 h = hits[i];
+        HitBest b;
+        b.t = h.x;
+        b.dt = 0.0f;
+        b.prim = __float_as_int(h.y);
+        b.undec = k_undec_none;
+        return b;
+    }
     __device__ __forceinline__ void load(int i, float3& o, float3& d, float& tmax, int& exclude) const {
         const float4 r0 = q[2 * i], r1 = q[2 * i + 1];
         o = xyz(r0);
@@ -177,20 +190,29 @@ struct ClosestJob {
         exclude = __float_as_int(r1.w);
     }
     __device__ __forceinline__ void store(int i, const TraceResult& s) const {
-        hits[i] = make_float4(s.t, __int_as_float(s.prim), s.u, s.v);
+        hits[i] = make_float4(s.t, __int_as_float(s.prim), 0.f, 0.f);
     }
 };
 
 // Shadow queue: sq[3i] = (origin, path id), sq[3i+1] = (direction, t_max), sq[3i+2] =
 // (contribution); an unoccluded ray adds its contribution to the path's radiance. The exact
-// segment of path pid is p.shadow_ff[3 pid].
+// segment of path pid is p.shadow_ff[3 pid]. A deferred ray found no certain occluder (it
+// would have stopped there), so its certain result is "unoccluded".
 struct ShadowJob {
     const float4* __restrict__ sq;
     PathDev p;
     DeferList deferred;
     __device__ __forceinline__ int pid(int i) const { return __float_as_int(sq[3 * i].w); }
     __device__ __forceinline__ ExactPtr exact(int i) const { return ExactPtr{p.shadow_ff + 3ull * pid(i)}; }
-    __device__ __forceinline__ void defer(int i) const { deferred.push(i); }
+    __device__ __forceinline__ void defer(int i, const TraceResult& r) const { deferred.push(i, r.undec); }
+    __device__ __forceinline__ HitBest partial(int i) const {
+        HitBest b;
+        b.t = sq[3 * i + 1].w;
+        b.dt = 0.0f;
+        b.prim = -1;
+        b.undec = k_undec_none;
+        return b;
+    }
     __device__ __forceinline__ void load(int i, float3& o, float3& d, float& tmax, int& exclude) const {
         const float4 r0 = sq[3 * i], r1 = sq[3 * i + 1];
         o = xyz(r0);
@@ -354,11 +376,12 @@ __device__ __forceinline__ float3 trace_path(const FrameParams& f, const SceneDe
     n_verts = 0;
     for (uint32_t k = 1; k <= f.max_depth; ++k) {
         const RayInv r = make_ray(ff3_f(ro), ff3_f(rd), pad);
-        float t, bu, bv;
         ++rays;
-        const int prim = trace_bvh<false, STATS, false, true>(s.nodes, s.tris, s.tri_in, s.n_tris, r,
-                                                              __int_as_float(0x7f800000), exclude, t, bu, bv, err, cnt,
-                                                              ExactRegs{ro, rd});
+        const HitBest hb = trace_bvh<false, STATS, false, true>(s.nodes, s.tris, s.tri_in, s.n_tris, r,
+                                                                __int_as_float(0x7f800000), exclude, err, cnt,
+                                                                ExactRegs{ro, rd});
+        const int prim = hb.prim;
+        const float t = hb.t;
         if (prim < 0) {
             sig = sig_mix(sig, k_sig_miss);
             break;
@@ -367,8 +390,8 @@ __device__ __forceinline__ float3 trace_path(const FrameParams& f, const SceneDe
         const float3 nb = beta * alb;
         const bool cont = k < f.max_depth && max3(nb) > 0.0f;
         VertexResult v;
-        shade_vertex(vs, path_key(f.seed, y * f.width + x, sample, k), prim, make_float4(t, 0.f, bu, bv), ro, rd, cont,
-                     v);
+        shade_vertex(vs, path_key(f.seed, y * f.width + x, sample, k), prim, make_float4(t, 0.f, 0.f, 0.f), ro, rd,
+                     cont, v);
         sig = sig_mix(sig, static_cast<uint32_t>(prim));
         if (k == 1) {
             const float3 em = xyz(__ldg(&s.emission[prim]));
@@ -378,10 +401,10 @@ __device__ __forceinline__ float3 trace_path(const FrameParams& f, const SceneDe
         float gv = 0.0f;
         if (v.nee) {
             const RayInv sr = make_ray(v.so, v.sd, pad);
-            float st2, su, sv;
             ++shadow_rays;
             const int occ = trace_bvh<true, STATS, false, true>(s.nodes, s.tris, s.tri_in, s.n_tris, sr, v.stmax, -1,
-                                                                st2, su, sv, err, cnt, ExactRegs{v.seg_o, v.seg_d});
+                                                                err, cnt, ExactRegs{v.seg_o, v.seg_d})
+                                .prim;
             if (occ < 0) {
                 // The same product and the same unfused add as the wavefront's shadow kernel.
                 const float3 cb = beta * alb * xyz(__ldg(&s.emission[v.light])) * v.g;

@@ -361,6 +361,11 @@ Q_CUDA_EXPORT int Q_cuda_batch_reset(Q_cuda_batch* batch) {
     return b->reset();
 }
 
+Q_CUDA_EXPORT int Q_cuda_batch_set_seed(Q_cuda_batch* batch, uint32_t seed, void* stream) {
+    Q_BATCH_OR_FAIL(batch);
+    return b->set_seed(seed, static_cast<cudaStream_t>(stream));
+}
+
 Q_CUDA_EXPORT int Q_cuda_batch_synchronize(Q_cuda_batch* batch) {
     Q_BATCH_OR_FAIL(batch);
     return b->synchronize();

@@ -14,9 +14,12 @@
 // from the exact path geometry: the double-float ray or shadow segment the path carries and
 // the triangle's original vertices (their differences are exact in double-float). The
 // re-decision agrees with FP64 except where the exact answer lies within ~1e-14 of a
-// boundary. Exact re-decisions are rare; the wavefront trace kernels do not make them
-// inline (one lane would hold up its warp for ~1000 instructions) but flag the ray, and a
-// small fixup kernel re-traces the flagged rays with inline re-decisions.
+// boundary. Exact re-decisions are rare (~1% of rays meet one undecided candidate); the
+// wavefront trace kernels do not make them inline (one lane would hold up its warp for ~1000
+// instructions) but record the undecided candidate and finish the traversal on the certain
+// decisions, culling only beyond the certain closest hit; a fixup kernel then re-decides the
+// recorded candidates with all lanes in step. A ray that meets a second undecided candidate
+// is re-traced whole with inline re-decisions.
 //
 // Error bound of the FP32 test (u = 2^-24; first order, each operation rounding once, FMA
 // contraction only removes roundings). Inputs: the FP32 ray (o, d) rounds the exact ray per
@@ -65,19 +68,19 @@ constexpr float k_seg_end_lo = 1.6593933338526767e-08f;     // (1 - 1e-4) - hi, 
 enum : int { k_tri_miss = 0, k_tri_hit = 1, k_tri_undecided = 2 };
 
 // FP32 Moller-Trumbore with its error bound. a = (v0, orig), e1 = (E1, K1), e2 = (E2, K2).
-// ANY: a shadow segment (its direction carries more rounding). Returns the class; t, dt
-// (t's error bound), u, v are set on every path.
+// ANY: a shadow segment (its direction carries more rounding). Returns the class; t and dt
+// (t's error bound) are set on every path.
 template <bool ANY>
-__device__ __forceinline__ int tri_classify(float3 o, float3 d, float4 a, float4 e1, float4 e2, float& t, float& dt,
-                                            float& u, float& v) {
+__device__ __forceinline__ int tri_classify(float3 o, float3 d, float4 a, float4 e1, float4 e2, float& t,
+                                            float& dt) {
     const float3 E1 = xyz(e1), E2 = xyz(e2);
     const float3 p = cross(d, E2);
     const float det = dot(E1, p);
     const float inv = 1.0f / det;  // det == 0 gives inf/nan: the bound is then inf/nan, undecided
     const float3 tv = o - xyz(a);
-    u = dot(tv, p) * inv;
+    const float u = dot(tv, p) * inv;
     const float3 q = cross(tv, E1);
-    v = dot(d, q) * inv;
+    const float v = dot(d, q) * inv;
     t = dot(E2, q) * inv;
     const float w = 1.0f - u - v;
     const float ainv = fabsf(inv);
@@ -95,10 +98,10 @@ __device__ __forceinline__ int tri_classify(float3 o, float3 d, float4 a, float4
 // Double-float Moller-Trumbore of the exact ray o + t d against the triangle with float
 // vertices v0, v1, v2 (its edges are exact in double-float). SEG: the ray is a shadow
 // segment (d = end - start) that counts only for t < 1 - 1e-4. Returns true on a hit with
-// t > 0 (and, SEG, t < 1 - 1e-4); t, u, v are then set. The signs decide, as the FP64
-// oracle's u < 0, u + v > 1, ... tests do.
+// t > 0 (and, SEG, t < 1 - 1e-4); t is then set. The signs decide, as the FP64 oracle's
+// u < 0, u + v > 1, ... tests do.
 template <bool SEG>
-__device__ __noinline__ bool exact_tri(ff3 o, ff3 d, float3 v0, float3 v1, float3 v2, ff& t, float& u, float& v) {
+__device__ __noinline__ bool exact_tri(ff3 o, ff3 d, float3 v0, float3 v1, float3 v2, ff& t) {
     const ff3 E1 = ff3_diff(v1, v0), E2 = ff3_diff(v2, v0);
     const ff3 p = ff3_cross(d, E2);
     const ff det = ff3_dot(E1, p);
@@ -120,8 +123,6 @@ __device__ __noinline__ bool exact_tri(ff3 o, ff3 d, float3 v0, float3 v1, float
         const ff diff = ff_sub(t, end);
         if (!(diff.hi < 0.0f)) return false;
     }
-    u = ff_f(ff_div(ud, det));
-    v = ff_f(ff_div(vd, det));
     return true;
 }
 
@@ -144,19 +145,24 @@ struct ExactRegs {
     }
 };
 
+// The undecided candidate a fast traversal recorded: none, or more than one (the ray is
+// then re-traced whole with inline re-decisions).
+constexpr int k_undec_none = -1;
+constexpr int k_undec_many = -2;
+
 // Closest-hit state of one ray (or the any-hit state of a shadow segment).
 struct HitBest {
-    float t;     // closest hit so far (t_max before any); box tests cull beyond t + dt
+    float t;     // closest certain hit so far (t_max before any); box tests cull beyond t + dt
     float dt;    // bound on |t - exact t| of the closest hit
     int prim;    // original index, or -1
-    float u, v;
+    int undec;   // fast traversal: the undecided candidate met (orig), k_undec_none or _many
 };
 
 // Re-decides candidate `orig` (vertices from the original-order triangle array) exactly and
 // updates `b`. Returns true when an any-hit query is answered (the segment is blocked).
-// When the candidate wins, its values come from the exact computation; when the incumbent
-// stays, its stored values are kept, so the result does not depend on the order in which
-// candidates are met.
+// When the candidate wins, its t comes from the exact computation; when the incumbent stays,
+// its stored t is kept, so the result does not depend on the order in which candidates are
+// met.
 template <bool ANY, class X>
 __device__ __noinline__ bool redecide(const float4* __restrict__ tri_in, const X& xr, int orig, HitBest& b) {
     ff3 o, d;
@@ -164,21 +170,18 @@ __device__ __noinline__ bool redecide(const float4* __restrict__ tri_in, const X
     const float3 a = xyz(__ldg(&tri_in[3 * orig])), bb = xyz(__ldg(&tri_in[3 * orig + 1])),
                  c = xyz(__ldg(&tri_in[3 * orig + 2]));
     ff t;
-    float u, v;
-    if (!exact_tri<ANY>(o, d, a, bb, c, t, u, v)) return false;
+    if (!exact_tri<ANY>(o, d, a, bb, c, t)) return false;
     if (ANY) {
         b.prim = orig;
-        b.t = ff_f(t);
         return true;
     }
     if (b.prim >= 0) {
         const float3 a2 = xyz(__ldg(&tri_in[3 * b.prim])), b2 = xyz(__ldg(&tri_in[3 * b.prim + 1])),
                      c2 = xyz(__ldg(&tri_in[3 * b.prim + 2]));
         ff tb;
-        float ub, vb;
         // The incumbent was decided as a hit; an exact miss here can only be a boundary case
         // within ~1e-14, where either answer is as good as FP64's.
-        if (exact_tri<false>(o, d, a2, b2, c2, tb, ub, vb)) {
+        if (exact_tri<false>(o, d, a2, b2, c2, tb)) {
             if (ff_less(tb, t) || (tb.hi == t.hi && tb.lo == t.lo && b.prim < orig)) return false;
         }
     }
@@ -186,8 +189,6 @@ __device__ __noinline__ bool redecide(const float4* __restrict__ tri_in, const X
     b.t = tf;
     b.dt = 2.0f * k_ulp * fabsf(tf);
     b.prim = orig;
-    b.u = u;
-    b.v = v;
     return false;
 }
 

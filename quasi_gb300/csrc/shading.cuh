@@ -57,7 +57,7 @@ __device__ __forceinline__ ff3 tri_unit_normal(const float4* __restrict__ tri_nr
     return ff3{ff{p.x, p.y}, ff{p.z, p.w}, ff{q.x, q.y}};
 }
 
-// hit: (t, prim, u, v) from the FP32 traversal; ro, rd: the double-float ray that found it.
+// hit: (t, prim, -, -) from the traversal; ro, rd: the double-float ray that found it.
 __device__ __forceinline__ void shade_vertex(const VertexScene& s, uint32_t key, int prim, float4 hit, const ff3& ro,
                                              const ff3& rd, bool want_dir, VertexResult& out) {
     // The light choice depends only on the path key: start its dependent loads (emitter
@@ -90,8 +90,9 @@ __device__ __forceinline__ void shade_vertex(const VertexScene& s, uint32_t key,
         const ff t = ff_div(ff3_dot(nrm, ff3_sub(ff3v(a), ro)), den);
         x = ff3_add(ro, ff3_scale(rd, t));
     } else {
-        const float3 e1 = xyz(__ldg(&s.tri_in[3 * prim + 1])) - a, e2 = xyz(__ldg(&s.tri_in[3 * prim + 2])) - a;
-        x = ff3v(a + e1 * hit.z + e2 * hit.w);
+        // A ray parallel to the plane cannot hit the triangle (an exact hit needs
+        // det = -d.(e1 x e2) != 0); kept only so that x is defined.
+        x = ff3v(a);
     }
     if (den.hi > 0.0f) nrm = ff3_neg(nrm);
     out.nrm = ff3_f(nrm);

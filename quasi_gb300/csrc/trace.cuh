@@ -10,8 +10,8 @@
 // exact tie goes to the smaller original triangle index. The oracle uses the same rule.
 // Hit decisions agree with exact arithmetic (robust.cuh): every FP32 triangle test carries
 // an error bound, boxes are padded by more than the slab planes' rounding, and box tests
-// cull beyond the closest hit's t plus its error bound. Undecided candidates either flag
-// the ray for the fixup kernel (fast mode) or are re-decided in double-float (ROBUST).
+// cull beyond the closest hit's t plus its error bound. Undecided candidates are either
+// recorded for the fixup kernel (fast mode) or re-decided in double-float (ROBUST).
 //
 // Traversal is written as a resumable step (one node visit) so persistent kernels can keep
 // every lane of a warp busy: a lane whose ray finishes takes a new ray from the queue while
@@ -34,10 +34,6 @@ constexpr int k_trace_steps = 8;
 // Measured on GB300 (soup 1M, 1080p): 5 levels is neutral, 7 slightly slower, 9 (32 KB per
 // block) 22% slower; the top levels are L1-resident either way.
 constexpr int k_default_smem_levels = 5;
-
-// Undecided-candidate marker in a trace result (fast mode): the ray is re-traced by the
-// fixup kernel with exact re-decisions.
-constexpr int k_prim_flagged = -2;
 
 // Spatial box padding Delta of the scene whose binary LBVH is `nodes`: 2^-16 times the
 // largest absolute vertex coordinate S (the root's child boxes hold every vertex). The
@@ -93,14 +89,18 @@ __device__ __forceinline__ HitBest hit_begin(float tmax) {
     // t_max of a shadow segment is FP32 (its length times 1 - 1e-4, a few roundings)
     b.dt = tmax < __int_as_float(0x7f800000) ? 8.0f * k_ulp * tmax : 0.0f;
     b.prim = -1;
-    b.u = b.v = 0.0f;
+    b.undec = k_undec_none;
     return b;
 }
 
 // Tests the triangle at leaf position `pos` (tris: leaf order {v0, orig}, {e1, K1},
-// {e2, K2}; tri_in: original-order vertices for re-decisions) and updates `b`. Returns true
-// when the traversal ends: an any-hit query is answered, or (fast mode) an undecided
-// candidate marks the result k_prim_flagged for the fixup kernel.
+// {e2, K2}) and updates `b`. Returns true when the traversal ends: an any-hit query is
+// answered, or (fast mode) a second undecided candidate was met.
+// Fast mode: an undecided candidate is recorded in b.undec and the traversal goes on with
+// the certain decisions (it culls only beyond the certain closest hit, so every triangle
+// that could beat it is still tested); the fixup kernel re-decides the record.
+// ROBUST: undecided candidates are re-decided inline from xr (the ray's exact geometry) and
+// tri_in (original-order vertices).
 template <bool ANY, bool ROBUST, class X>
 __device__ __forceinline__ bool leaf_test(const float4* __restrict__ tris, const float4* __restrict__ tri_in,
                                           const X& xr, const RayInv& r, uint32_t pos, int exclude, HitBest& b) {
@@ -108,16 +108,15 @@ __device__ __forceinline__ bool leaf_test(const float4* __restrict__ tris, const
     const float4 a = __ldg(p), e1 = __ldg(p + 1), e2 = __ldg(p + 2);
     const int orig = __float_as_int(a.w);
     if (orig == exclude) return false;
-    float t, dt, u, v;
-    const int c = tri_classify<ANY>(r.o, r.d, a, e1, e2, t, dt, u, v);
+    float t, dt;
+    const int c = tri_classify<ANY>(r.o, r.d, a, e1, e2, t, dt);
     if (c == k_tri_miss) return false;
     if (c == k_tri_hit) {
         if (t + dt < b.t - b.dt) {  // certainly closer than the closest so far (inside t_max)
             b.t = t;
             b.dt = dt;
             b.prim = orig;
-            b.u = u;
-            b.v = v;
+            if (ANY) b.undec = k_undec_none;  // a certain occluder answers the query
             return ANY;
         }
         if (t - dt > b.t + b.dt) return false;  // certainly farther
@@ -125,7 +124,11 @@ __device__ __forceinline__ bool leaf_test(const float4* __restrict__ tris, const
     if constexpr (ROBUST) {
         return redecide<ANY>(tri_in, xr, orig, b);
     } else {
-        b.prim = k_prim_flagged;
+        if (b.undec == k_undec_none) {
+            b.undec = orig;
+            return false;
+        }
+        b.undec = k_undec_many;
         return true;
     }
 }
@@ -140,14 +143,15 @@ struct TraceCounters {
     uint32_t tris = 0;
 };
 
-// Result of one traversal: prim = original index of the closest hit, -1 for none, or
-// k_prim_flagged (fast mode: re-trace in the fixup kernel).
+// Result of one traversal: prim = original index of the closest certain hit or -1; undec =
+// the undecided candidate the fixup kernel must re-decide (k_undec_none: the result is final;
+// k_undec_many: re-trace the ray whole).
 struct TraceResult {
     float t;
     int prim;
-    float u, v;
+    int undec;
 };
-__device__ __forceinline__ TraceResult trace_result(const HitBest& b) { return TraceResult{b.t, b.prim, b.u, b.v}; }
+__device__ __forceinline__ TraceResult trace_result(const HitBest& b) { return TraceResult{b.t, b.prim, b.undec}; }
 
 // Per-ray traversal state of the resumable binary traversal (the stack lives beside it).
 struct TraceState {
@@ -228,9 +232,9 @@ __device__ __forceinline__ bool trace_step(const float4* __restrict__ nodes, con
 
 // Whole-ray traversal for kernels that trace one ray at a time.
 // ANY = true: stops at the first hit with t in (0, tmax) and returns a prim >= 0.
-// Returns the original index of the hit triangle (or -1; k_prim_flagged in fast mode when an
-// undecided candidate was met), its distance in t_out and its barycentrics in bu, bv.
-// ROBUST: undecided candidates are re-decided exactly from xr (exact ray) and tri_in.
+// Returns the traversal's final state: the closest (certain) hit and, in fast mode, the
+// undecided candidate it recorded. ROBUST: undecided candidates are re-decided exactly from
+// xr (the exact ray) and tri_in, so the result is final.
 // Treelet nodes (the top levels copied to shared memory) are addressed as k_tree_flag | i.
 constexpr int k_tree_flag = 0x40000000;
 
@@ -239,17 +243,12 @@ constexpr int k_tree_flag = 0x40000000;
 // the traversal starts in `tree` (shared memory), whose child links point into the treelet
 // (k_tree_flag) or out to global nodes.
 template <bool ANY, bool STATS, bool TREE = false, bool ROBUST = false, class X = ExactNone>
-__device__ __forceinline__ int trace_bvh(const float4* __restrict__ nodes, const float4* __restrict__ tris,
-                                         const float4* __restrict__ tri_in, uint32_t n_tris, const RayInv& r,
-                                         float tmax, int exclude, float& t_out, float& bu, float& bv, uint32_t& err,
-                                         TraceCounters& cnt, const X& xr = X{}, const float4* tree = nullptr,
-                                         int tree_n = 0) {
+__device__ __forceinline__ HitBest trace_bvh(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                                             const float4* __restrict__ tri_in, uint32_t n_tris, const RayInv& r,
+                                             float tmax, int exclude, uint32_t& err, TraceCounters& cnt,
+                                             const X& xr = X{}, const float4* tree = nullptr, int tree_n = 0) {
     HitBest b = hit_begin(tmax);
-    if (n_tris == 0) {
-        t_out = b.t;
-        bu = bv = 0.0f;
-        return -1;
-    }
+    if (n_tris == 0) return b;
     int stack[k_stack_size];
     int sp = 0;
     int node = (TREE && tree_n > 0) ? k_tree_flag : 0;
@@ -313,17 +312,15 @@ __device__ __forceinline__ int trace_bvh(const float4* __restrict__ nodes, const
             node = stack[--sp];
         }
     }
-    t_out = b.t;
-    bu = b.u;
-    bv = b.v;
-    return b.prim;
+    return b;
 }
 
-// Hands one finished ray to the job: a flagged ray goes to the fixup list, others store.
+// Hands one finished ray to the job: a ray with an undecided candidate goes to the fixup
+// list (with its certain result), others store their final result.
 template <class Job>
 __device__ __forceinline__ void finish_ray(Job& job, int i, const TraceResult& res) {
-    if (res.prim == k_prim_flagged)
-        job.defer(i);
+    if (res.undec != k_undec_none)
+        job.defer(i, res);
     else
         job.store(i, res);
 }
@@ -333,7 +330,7 @@ __device__ __forceinline__ void finish_ray(Job& job, int i, const TraceResult& r
 // tree/tree_n: the treelet in shared memory (used when TREE). Job supplies
 //   void load(int i, float3& o, float3& d, float& tmax, int& exclude)
 //   void store(int i, const TraceResult& r)
-//   void defer(int i)        (the ray met an undecided candidate: re-trace it exactly)
+//   void defer(int i, const TraceResult& r)   (r.undec needs an exact re-decision)
 template <bool ANY, bool STATS, bool TREE, class Job>
 __device__ __forceinline__ void trace_batches(Job& job, const float4* __restrict__ nodes,
                                               const float4* __restrict__ tris, uint32_t n_tris, int n,
@@ -353,10 +350,9 @@ __device__ __forceinline__ void trace_batches(Job& job, const float4* __restrict
             int exclude;
             job.load(i, o, d, tmax, exclude);
             const RayInv r = make_ray(o, d, pad);
-            TraceResult res;
-            res.prim = trace_bvh<ANY, STATS, TREE>(nodes, tris, nullptr, n_tris, r, tmax, exclude, res.t, res.u, res.v,
-                                                   err, cnt, ExactNone{}, tree, tree_n);
-            finish_ray(job, i, res);
+            finish_ray(job, i,
+                       trace_result(trace_bvh<ANY, STATS, TREE>(nodes, tris, nullptr, n_tris, r, tmax, exclude, err,
+                                                                cnt, ExactNone{}, tree, tree_n)));
         }
     }
 }
@@ -408,16 +404,17 @@ __device__ __forceinline__ void trace_persistent(Job& job, const float4* __restr
     }
 }
 
-// Re-traces the rays a fast trace kernel deferred (list[0 .. *count)) with exact
-// re-decisions over the binary LBVH, one ray per thread, warps taking 32 list entries per
-// atomic. Job supplies load, store and exact(i) (the ray's exact geometry).
+// Completes the rays a fast trace kernel deferred: entry k of `list` is (ray i, its
+// undecided candidate). One entry per thread, 32 entries per warp and atomic, so the exact
+// re-decisions run with the lanes in step. A candidate is re-decided against the ray's
+// certain result (job.partial(i)); a ray that met more than one is re-traced whole over the
+// binary LBVH with inline re-decisions. Job supplies load, store, partial(i) and exact(i).
 template <bool ANY, class Job>
-__device__ __forceinline__ void trace_fixups(Job& job, const float4* __restrict__ nodes,
-                                             const float4* __restrict__ tris, const float4* __restrict__ tri_in,
-                                             uint32_t n_tris, const int* __restrict__ list, int n,
-                                             int* __restrict__ fetch, uint32_t& err) {
+__device__ __forceinline__ void resolve_deferred(Job& job, const float4* __restrict__ nodes,
+                                                 const float4* __restrict__ tris, const float4* __restrict__ tri_in,
+                                                 uint32_t n_tris, const int2* __restrict__ list, int n,
+                                                 int* __restrict__ fetch, uint32_t& err) {
     const int lane = threadIdx.x & 31;
-    const float pad = n_tris ? scene_box_pad(nodes) : 0.0f;
     TraceCounters cnt;
     while (true) {
         int base = 0;
@@ -426,16 +423,23 @@ __device__ __forceinline__ void trace_fixups(Job& job, const float4* __restrict_
         if (base >= n) break;
         const int k = base + lane;
         if (k < n) {
-            const int i = list[k];
-            float3 o, d;
-            float tmax;
-            int exclude;
-            job.load(i, o, d, tmax, exclude);
-            const RayInv r = make_ray(o, d, pad);
-            TraceResult res;
-            res.prim = trace_bvh<ANY, false, false, true>(nodes, tris, tri_in, n_tris, r, tmax, exclude, res.t, res.u,
-                                                          res.v, err, cnt, job.exact(i));
-            job.store(i, res);
+            const int2 e = list[k];
+            const int i = e.x;
+            HitBest b;
+            if (e.y == k_undec_many) {
+                float3 o, d;
+                float tmax;
+                int exclude;
+                job.load(i, o, d, tmax, exclude);
+                const RayInv r = make_ray(o, d, n_tris ? scene_box_pad(nodes) : 0.0f);
+                b = trace_bvh<ANY, false, false, true>(nodes, tris, tri_in, n_tris, r, tmax, exclude, err, cnt,
+                                                       job.exact(i));
+            } else {
+                b = job.partial(i);
+                redecide<ANY>(tri_in, job.exact(i), e.y, b);
+            }
+            b.undec = k_undec_none;
+            job.store(i, trace_result(b));
         }
     }
 }

@@ -249,8 +249,8 @@ int Renderer::ensure_frame_buffers(uint32_t w, uint32_t h) {
 
 // Bytes of wave state per path slot: two ray queues (2 x 32), hit 16, shadow ray 48, beta,
 // radiance and two AOVs (4 x 16), signature 4, double-float ray 48, exact shadow segment 48,
-// fixup list entry 4.
-constexpr size_t k_wave_bytes_per_path = 296;
+// fixup list entry 8.
+constexpr size_t k_wave_bytes_per_path = 300;
 
 int Renderer::ensure_wave_buffers(uint32_t paths) {
     if (paths <= wave_capacity_) return QUASI_OK;
@@ -265,7 +265,7 @@ int Renderer::ensure_wave_buffers(uint32_t paths) {
     R_TRY(sig_.reserve(sizeof(uint32_t) * paths), "sig");
     R_TRY(ray_ff_.reserve(sizeof(float4) * 3ull * paths), "ray_ff");
     R_TRY(shadow_ff_.reserve(sizeof(float4) * 3ull * paths), "shadow_ff");
-    R_TRY(defer_.reserve(sizeof(int) * paths), "defer");
+    R_TRY(defer_.reserve(sizeof(int2) * paths), "defer");
     wave_capacity_ = paths;
     return QUASI_OK;
 }
@@ -419,11 +419,7 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
     const int grid_c = sm_count_ * std::max(occ_c, 1);
     const int grid_s = sm_count_ * std::max(occ_s, 1);
     const int grid_shade = sm_count_ * 8;
-    int occ_f = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, k_fixup<ClosestJob>, 256, wide_stack_smem_bytes<true>(256));
-    const int grid_fixup = sm_count_ * std::max(occ_f, 1);
-    const size_t smem_fc = wide ? wide_stack_smem_bytes<false>(256) : 0;
-    const size_t smem_fs = wide ? wide_stack_smem_bytes<true>(256) : 0;
+    const int grid_fixup = sm_count_ * 4;
     uint32_t* err = err_dev_.as<uint32_t>();
     unsigned long long* st = stats_dev_.as<unsigned long long>();
     const uint32_t px = width_ * height_;
@@ -448,13 +444,13 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
             int* f_cur = cnt + 2 * D + (k - 1);
             int* f_shadow = cnt + 3 * D + (k - 1);
             const ClosestJob cjob{qcur, hits_.as<float4>(), ray_ff_.as<float4>(),
-                                  DeferList{defer_.as<int>(), cnt + 4 * D + (k - 1)}};
-            const ShadowJob sjob{shadow_.as<float4>(), pd, DeferList{defer_.as<int>(), cnt + 5 * D + (k - 1)}};
+                                  DeferList{defer_.as<int2>(), cnt + 4 * D + (k - 1)}};
+            const ShadowJob sjob{shadow_.as<float4>(), pd, DeferList{defer_.as<int2>(), cnt + 5 * D + (k - 1)}};
             R_TRY(QUASI_LAUNCH(prof_, "trace_closest", s,
                                (kc<<<grid_c, tb, smem_c, s>>>(sd, cjob, c_cur, cap, f_cur, err, st))),
                   "trace_closest");
             R_TRY(QUASI_LAUNCH(prof_, "fixup_closest", s,
-                               (k_fixup<ClosestJob><<<grid_fixup, 256, smem_fc, s>>>(sd, cjob, cnt + 6 * D + (k - 1), err))),
+                               (k_fixup<ClosestJob><<<grid_fixup, 128, 0, s>>>(sd, cjob, cnt + 6 * D + (k - 1), err))),
                   "fixup_closest");
             R_TRY(QUASI_LAUNCH(prof_, "shade", s,
                                (k_shade<<<grid_shade, 256, 0, s>>>(f, sd, pd, k, qcur, hits_.as<float4>(), c_cur, cap, qnext,
@@ -465,7 +461,7 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
                                (ks<<<grid_s, tb, smem_s, s>>>(sd, sjob, c_shadow, cap, f_shadow, err, st))),
                   "trace_shadow");
             R_TRY(QUASI_LAUNCH(prof_, "fixup_shadow", s,
-                               (k_fixup<ShadowJob><<<grid_fixup, 256, smem_fs, s>>>(sd, sjob, cnt + 7 * D + (k - 1), err))),
+                               (k_fixup<ShadowJob><<<grid_fixup, 128, 0, s>>>(sd, sjob, cnt + 7 * D + (k - 1), err))),
                   "fixup_shadow");
         }
         R_TRY(QUASI_LAUNCH(prof_, "accumulate", s,

@@ -102,23 +102,16 @@ __global__ void __launch_bounds__(256, trace_min_blocks(MODE)) k_trace_shadow(Sc
     flush_counters<STATS>(c, stats + 2);
 }
 
-// Re-traces the rays a closest-hit or shadow trace kernel deferred (an undecided candidate:
-// robust.cuh) over the 8-wide records with per-lane refill, re-deciding undecided candidates
-// exactly, and stores their results. The list length is read on the device, so the launch
-// needs no host synchronisation. Launched like the trace kernels (shared-memory stacks).
+// Completes the rays a closest-hit or shadow trace kernel deferred (robust.cuh): re-decides
+// each ray's recorded candidate exactly against its certain result, or re-traces a ray that
+// met more than one, and stores the final results. The list length is read on the device, so
+// the launch needs no host synchronisation; a persistent grid takes 32 entries per warp.
 template <class Job>
-__global__ void __launch_bounds__(256, 2) k_fixup(SceneDev s, Job job, int* __restrict__ fetch,
-                                                                     uint32_t* __restrict__ err) {
+__global__ void __launch_bounds__(128) k_fixup(SceneDev s, Job job, int* __restrict__ fetch,
+                                               uint32_t* __restrict__ err) {
     constexpr bool any = std::is_same<Job, ShadowJob>::value;
     uint32_t e = 0;
-    TraceCounters c;
-    FixupJob<Job> fj{job, job.deferred.list};
-    const int n = *job.deferred.count;
-    if (s.wide)
-        trace_wide_refill<any, false, FixupJob<Job>, true>(fj, s.wide, s.tris, s.n_tris, n, k_wide_refill_lanes, fetch,
-                                                           e, c, s.tri_in);
-    else
-        trace_fixups<any>(job, s.nodes, s.tris, s.tri_in, s.n_tris, job.deferred.list, n, fetch, e);
+    resolve_deferred<any>(job, s.nodes, s.tris, s.tri_in, s.n_tris, job.deferred.list, *job.deferred.count, fetch, e);
     if (e) atomicOr(err, e);
 }
 

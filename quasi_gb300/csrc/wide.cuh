@@ -32,13 +32,10 @@
 // Closest hit is the smallest t, and an exact tie goes to the smaller original index, as in
 // the binary traversal (trace.cuh), so both return the same triangle. Child boxes are padded
 // by the scene's Delta (scene_box_pad) before quantisation, and triangle tests classify
-// their candidates (robust.cuh): a ray that meets an undecided candidate ends with
-// k_prim_flagged and is re-traced exactly by the fixup kernel.
+// their candidates (robust.cuh): an undecided candidate is recorded for the fixup kernel.
 #pragma once
 
 #include "trace.cuh"
-
-#include <type_traits>
 
 namespace quasi {
 
@@ -187,15 +184,12 @@ __device__ __forceinline__ float fmin3(float a, float b, float c) {
 // Tests the triangle of one leaf (one-triangle leaves: a leaf that passed its box test
 // holds exactly one triangle, empty slots never pass); returns true when the traversal ends
 // (an any-hit query answered, or an undecided candidate flagged the ray).
-// ROBUST: undecided candidates are re-decided exactly (tri_in: original-order vertices, xr:
-// the ray's exact geometry) instead of ending the traversal.
-template <bool ANY, bool STATS, bool ROBUST = false, class X = ExactNone>
+template <bool ANY, bool STATS>
 __device__ __forceinline__ bool wide_leaf(const float4* __restrict__ tris, const RayInv& r, int ref, int exclude,
-                                          HitBest& b, TraceCounters& cnt, const float4* __restrict__ tri_in = nullptr,
-                                          const X& xr = X{}) {
+                                          HitBest& b, TraceCounters& cnt) {
     static_assert(k_wide_leaf_max == 1, "wide_leaf tests one triangle per leaf");
     if (STATS) ++cnt.tris;
-    return leaf_test<ANY, ROBUST>(tris, tri_in, xr, r, static_cast<uint32_t>(~ref) >> 2, exclude, b);
+    return leaf_test<ANY, false>(tris, nullptr, ExactNone{}, r, static_cast<uint32_t>(~ref) >> 2, exclude, b);
 }
 
 // Traversal state of one ray over the 8-wide records (the stack lives beside it).
@@ -203,7 +197,7 @@ struct WideRay {
     RayInv r;
     uint32_t oct;   // direction octant: bit a set where component a is negative
     int exclude;
-    HitBest b;      // closest hit so far (prim k_prim_flagged: undecided, re-trace exactly)
+    HitBest b;      // closest certain hit so far and the undecided candidate met, if any
     int node;       // record to visit next, or k_wide_done
     int sp;
     uint32_t budget;
@@ -238,10 +232,9 @@ __device__ __forceinline__ int wide_pop(WideRay& q, const Stack& stack) {
 // visit and stacking the other leaves (each loop turn then costs one triangle test, not the
 // busiest lane's count) was measured 7% slower on the 1M soup: the extra stack traffic and
 // loop turns cost more than the divergence they remove.
-template <bool ANY, bool STATS, class Stack, bool ROBUST = false, class X = ExactNone>
+template <bool ANY, bool STATS, class Stack>
 __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, const float4* __restrict__ tris,
-                                           WideRay& q, Stack& stack, uint32_t& err, TraceCounters& cnt,
-                                           const float4* __restrict__ tri_in = nullptr, const X& xr = X{}) {
+                                           WideRay& q, Stack& stack, uint32_t& err, TraceCounters& cnt) {
     if (q.node == k_wide_done) return true;
     if (--q.budget == 0u) {
         err |= k_deverr_traversal;
@@ -315,7 +308,7 @@ __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, cons
     while (lm) {
         const uint32_t s = __ffs(lm) - 1;
         lm &= lm - 1u;
-        if (wide_leaf<ANY, STATS, ROBUST>(tris, r, sel8(refs, s), q.exclude, q.b, cnt, tri_in, xr)) {
+        if (wide_leaf<ANY, STATS>(tris, r, sel8(refs, s), q.exclude, q.b, cnt)) {
             q.node = k_wide_done;
             return true;
         }
@@ -366,8 +359,8 @@ __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, cons
 }
 
 // Whole-ray traversal of the 8-wide BVH (fast mode); same contract as trace_bvh
-// (trace.cuh): ANY = true stops at the first hit with t in (0, tmax); prim is the original
-// index of the hit triangle, -1, or k_prim_flagged when an undecided candidate was met.
+// (trace.cuh): ANY = true stops at the first certain hit with t in (0, tmax); the result
+// carries the undecided candidate met, if any.
 template <bool ANY, bool STATS>
 __device__ __forceinline__ TraceResult trace_wide(const float4* __restrict__ wide, const float4* __restrict__ tris,
                                                   uint32_t n_tris, float3 o, float3 d, float tmax, int exclude,
@@ -408,19 +401,14 @@ __device__ __forceinline__ void trace_batches_wide(Job& job, const float4* __res
 // their own rays (refill = 32 waits for the whole warp). Job as in trace_batches. Every
 // lane of the warp must call this (it uses full-warp votes), and the block must be launched
 // with wide_stack_smem_bytes<ANY>(blockDim.x) of dynamic shared memory.
-// ROBUST (the fixup kernels): undecided candidates are re-decided inline from the job's
-// exact(i) geometry and the original-order vertices tri_in, and every ray is stored.
-template <bool ANY, bool STATS, class Job, bool ROBUST = false>
+template <bool ANY, bool STATS, class Job>
 __device__ __forceinline__ void trace_wide_refill(Job& job, const float4* __restrict__ wide,
                                                   const float4* __restrict__ tris, uint32_t n_tris, int n, int refill,
-                                                  int* __restrict__ fetch, uint32_t& err, TraceCounters& cnt,
-                                                  const float4* __restrict__ tri_in = nullptr) {
+                                                  int* __restrict__ fetch, uint32_t& err, TraceCounters& cnt) {
     const int lane = threadIdx.x & 31;
     WideRay q;
     WideStack<wide_smem_stack<ANY>()> stack;
     stack.slot = wide_stack_slot<ANY>();
-    using X = typename std::conditional<ROBUST, ExactPtr, ExactNone>::type;
-    X xr{};
     bool active = false, exhausted = false;
     int idx = 0;
     while (true) {
@@ -438,7 +426,6 @@ __device__ __forceinline__ void trace_wide_refill(Job& job, const float4* __rest
                     float tmax;
                     int exclude;
                     job.load(idx, o, d, tmax, exclude);
-                    if constexpr (ROBUST) xr = job.exact(idx);
                     wide_begin(q, o, d, tmax, exclude, n_tris);
                     active = true;
                 }
@@ -449,32 +436,15 @@ __device__ __forceinline__ void trace_wide_refill(Job& job, const float4* __rest
         if (active) {
 #pragma unroll 1
             for (int i = 0; i < k_wide_visits_per_check; ++i) {
-                done = wide_visit<ANY, STATS, WideStack<wide_smem_stack<ANY>()>, ROBUST>(wide, tris, q, stack, err, cnt,
-                                                                                       tri_in, xr);
+                done = wide_visit<ANY, STATS>(wide, tris, q, stack, err, cnt);
                 if (done) break;
             }
         }
         if (done) {
-            if constexpr (ROBUST)
-                job.store(idx, trace_result(q.b));
-            else
-                finish_ray(job, idx, trace_result(q.b));
+            finish_ray(job, idx, trace_result(q.b));
             active = false;
         }
     }
 }
-
-// A job over the entries of a fixup list: entry k is ray list[k] of the underlying job.
-template <class Job>
-struct FixupJob {
-    Job job;
-    const int* __restrict__ list;
-    __device__ __forceinline__ void load(int k, float3& o, float3& d, float& tmax, int& exclude) const {
-        job.load(list[k], o, d, tmax, exclude);
-    }
-    __device__ __forceinline__ void store(int k, const TraceResult& r) const { job.store(list[k], r); }
-    __device__ __forceinline__ ExactPtr exact(int k) const { return job.exact(list[k]); }
-    __device__ __forceinline__ int pid(int k) const { return job.pid(list[k]); }
-};
 
 }  // namespace quasi

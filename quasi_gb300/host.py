@@ -392,6 +392,10 @@ class Batch:
     def reset(self) -> None:
         self._check("Q_cuda_batch_reset", self.lib.Q_cuda_batch_reset(self.handle))
 
+    def set_seed(self, seed: int, stream: int | None = None) -> None:
+        """New RNG seed for every scene (device-side; the captured graphs stay valid)."""
+        self._check("Q_cuda_batch_set_seed", self.lib.Q_cuda_batch_set_seed(self.handle, seed, stream))
+
     def synchronize(self) -> None:
         self._check("Q_cuda_batch_synchronize", self.lib.Q_cuda_batch_synchronize(self.handle))
 

@@ -1,6 +1,7 @@
-"""Path-replay adjoint: gradients of an L2 image loss with respect to per-triangle albedo and
-emission, against the FP64 oracle's analytic gradient and against central finite differences
-(eps 1e-3) of the GPU forward renderer; plus megakernel/wavefront identity.
+"""Path-replay adjoint: gradients of an L2 image loss with respect to per-triangle albedo
+against central finite differences (eps 1e-3) of the GPU forward renderer; plus
+megakernel/wavefront identity. The FP64 oracle gradient and the emission differences are
+checked at the differentiation configuration in test_gpu_configs.py.
 
 Tolerance: relative error <= 1e-3 on every checked gradient entry.
 """
@@ -39,28 +40,6 @@ def _setup(torch, spec, w, h, spp, depth):
     with torch.no_grad():
         target = qa.render(target_alb, emission.detach(), host, w, h, spp).clone()
     return qa, scene, host, albedo, emission, target
-
-
-def test_adjoint_matches_fp64_oracle_gradient(torch_mod, orc):
-    torch = torch_mod
-    w = h = 128
-    spp, depth = 16, 4
-    qa, scene, host, albedo, emission, target = _setup(torch, "soup:n=10000,seed=7", w, h, spp, depth)
-    img = qa.render(albedo, emission, host, w, h, spp)
-    loss = ((img - target) ** 2).mean()
-    loss.backward()
-    ga = albedo.grad.cpu().numpy().astype(np.float64)
-    ge = emission.grad.cpu().numpy().astype(np.float64)
-    grad_image = (2.0 * (img - target) / img.numel()).detach().cpu().numpy().astype(np.float64)
-    oa, oe = orc.backward(scene, w, h, spp, depth, grad_image, seed=0)
-    for got, ref, name in ((ga, oa, "albedo"), (ge, oe, "emission")):
-        big = np.abs(ref) > 1e-3 * np.abs(ref).max()
-        assert big.sum() > 20, name
-        rel = np.abs(got[big] - ref[big]) / np.abs(ref[big])
-        # a path whose FP32 traversal decision differs from FP64 can move a few entries
-        assert np.quantile(rel, 0.99) <= GRAD_TOL, (name, np.sort(rel)[-5:])
-        assert np.median(rel) <= 1e-5, (name, np.median(rel))
-    host.destroy()
 
 
 def test_adjoint_matches_central_finite_differences(torch_mod):

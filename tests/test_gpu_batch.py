@@ -197,12 +197,10 @@ def test_batch_rejects_bad_input(scenes):
 
 
 def test_batch_fit_recovers_albedo(scenes):
-    """Batched differentiation: Adam on the albedo of 3 scenes against images rendered with the
-    true albedo (same seeds) drives the loss down and reduces the albedo error of the triangles
-    seen. At 3-16 spp many triangles lie on only a few paths, where the image constrains a
-    product of several albedos, not each one: the loss falls by orders of magnitude while the
-    error of all seen triangles falls by about a quarter (0.099 -> 0.074 after 30 steps on a
-    GB300), and by about half for the tenth of triangles with the largest gradients."""
+    """Batched differentiation: Adam on the albedo of 3 scenes. Every step re-seeds the batch
+    and renders its target from the true albedo with that seed, so the fit sees new paths each
+    step (with one fixed set of paths the image constrains products of the albedos along them,
+    not each albedo). The loss falls and the albedo error of the triangles seen falls."""
     torch = pytest.importorskip("torch")
     from quasi_gb300 import autograd as qa
 
@@ -217,18 +215,16 @@ def test_batch_fit_recovers_albedo(scenes):
         target = qa.render_batch(gt, em, batch).clone()
     a0 = init.clone().requires_grad_(True)
     ((qa.render_batch(a0, em, batch) - target) ** 2).mean().backward()
-    gmag = a0.grad.abs().sum(dim=1)
-    seen = gmag > 0
+    seen = a0.grad.abs().sum(dim=1) > 0
     assert int(seen.sum()) > 50
-    top = gmag >= torch.quantile(gmag[seen], 0.9)
-    fitted, losses = qa.fit_albedo(batch, target, init, em, steps=30, lr=0.01)
-    assert losses[-1] < 0.05 * losses[0], (losses[0], losses[-1])
+    fitted, losses = qa.fit_albedo(batch, None, init, em, steps=40, lr=0.01, target_albedo=gt, seed0=1)
+    assert losses[-1] < 0.5 * losses[0], (losses[0], losses[-1])
 
     def rmse(a, m):
         return float(((a - gt)[m] ** 2).mean().sqrt())
 
-    assert rmse(fitted, seen) < 0.85 * rmse(init, seen), (rmse(init, seen), rmse(fitted, seen))
-    assert rmse(fitted, top) < 0.7 * rmse(init, top), (rmse(init, top), rmse(fitted, top))
+    print(f"albedo RMSE over seen triangles {rmse(init, seen):.4f} -> {rmse(fitted, seen):.4f}")
+    assert rmse(fitted, seen) < 0.7 * rmse(init, seen), (rmse(init, seen), rmse(fitted, seen))
     st = batch.stats()
     assert st.error_flags == 0 and st.adjoint_rays > 0
     batch.destroy()

@@ -9,12 +9,14 @@ than FP64 takes.
 from __future__ import annotations
 
 import ctypes
+import json
 
 import numpy as np
 import pytest
 
 import quasi_gb300 as q
 from quasi_gb300 import _abi as A
+from tests.parity_stats import error_stats
 
 pytestmark = pytest.mark.gpu
 
@@ -45,7 +47,15 @@ def _rel(a, b):
     return np.abs(a - b) / np.maximum(np.abs(b), FLOOR)
 
 
-def _check_parity(img, rad, sig, ref, w, h, spp):
+def _report(name, g_img, g_rad, g_sig, ref, spp):
+    """Prints the error statistics of one workload (shown with pytest -s)."""
+    st = error_stats(g_img, g_rad, g_sig, ref["mean"], ref["samples"], ref["sig"], spp)
+    print(json.dumps({"workload": name, **st}))
+    return st
+
+
+def _check_parity(img, rad, sig, ref, w, h, spp, name=""):
+    _report(name, img[..., :3], rad, sig, ref, spp)
     osig = ref["sig"].reshape(h, w, spp)
     osamp = ref["samples"].reshape(h, w, spp, 3)
     match = sig == osig
@@ -66,7 +76,7 @@ def test_cornell36_parity(host, orc):
     scene = q.make_scene("cornell36", host.lib)
     img, rad, sig, st = _render(host, scene, w, h, spp, depth)
     ref = orc.render_nee(scene, w, h, spp, depth, seed=0, want_samples=True)
-    _check_parity(img, rad, sig, ref, w, h, spp)
+    _check_parity(img, rad, sig, ref, w, h, spp, name="cornell36 256x256 16spp depth4")
     assert st.camera_rays == w * h * spp
     # every path takes the oracle's branches, so the ray counts are the oracle's exactly
     for k, v in (("camera", st.camera_rays), ("extension", st.extension_rays), ("shadow", st.shadow_rays)):
@@ -80,7 +90,7 @@ def test_refcornell_triangles_parity(host, orc):
     scene = q.make_scene("refcornell", host.lib)
     img, rad, sig, _ = _render(host, scene, w, h, spp, depth, seed=7)
     ref = orc.render_nee(scene, w, h, spp, depth, seed=7, want_samples=True)
-    _check_parity(img, rad, sig, ref, w, h, spp)
+    _check_parity(img, rad, sig, ref, w, h, spp, name="refcornell 96x72 8spp depth5")
 
 
 def test_soup_parity_subset(host, orc):
@@ -95,6 +105,7 @@ def test_soup_parity_subset(host, orc):
     ys, xs = pix // w, pix % w
     g_sig = sig[ys, xs]
     g_rad = rad[ys, xs].astype(np.float64)
+    _report("soup-100k 320x180 4spp depth8 (1500 random pixels)", img[ys, xs, :3], g_rad, g_sig, ref, spp)
     match = g_sig == ref["sig"]
     assert match.all(), np.argwhere(~match)[:8]
     assert _rel(g_rad, ref["samples"]).max() <= REL_TOL
@@ -399,6 +410,7 @@ def test_benchmark_frame_parity_sampled_pixels(orc):
     pix = rng.choice(w * h, size=200, replace=False).astype(np.uint32)
     ref = orc.render_nee(scene, w, h, spp, depth, seed=17, pixels=pix, want_samples=True)
     ys, xs = pix // w, pix % w
+    _report("soup-1M 1920x1080 64spp depth8 (200 random pixels)", img[ys, xs, :3], rad[ys, xs], sig[ys, xs], ref, spp)
     match = sig[ys, xs] == ref["sig"]
     assert match.all(), np.argwhere(~match)[:8]
     assert _rel(rad[ys, xs].astype(np.float64), ref["samples"]).max() <= REL_TOL

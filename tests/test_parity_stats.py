@@ -1,11 +1,11 @@
-"""The error statistics of tests/parity_report.py on planted data (CPU): divergent pixels
-are kept out of the max and percentile, and counted apart."""
+"""The parity statistics helper (tests/parity_stats.py) on planted data (CPU): divergent
+pixels are kept out of the max and percentile, and counted apart."""
 from __future__ import annotations
 
 import numpy as np
 import pytest
 
-pr = pytest.importorskip("tests.parity_report", reason="needs the package importable")
+pr = pytest.importorskip("tests.parity_stats", reason="needs the tests package importable")
 
 
 def test_error_stats_split_divergent_pixels():
