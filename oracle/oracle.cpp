@@ -24,6 +24,9 @@
 #include <cstdint>
 #include <cstring>
 #include <limits>
+#include <random>
+#include <string>
+#include <cstdlib>
 #include <thread>
 #include <vector>
 
@@ -1043,6 +1046,230 @@ ORACLE_API int oracle_render_reference(uint32_t nq, const float* quads, const fl
         if (out_aov)
             for (int k = 0; k < 7; ++k) out_aov[7ull * i + k] = as[k] / cfg->spp;
     });
+    return 0;
+}
+
+// ---------------------------------------------------------------- benchmark scenes
+//
+// The library's built-in scenes (quasi_gb300/csrc/scene.cpp, Q_cuda_make_scene) restated so
+// the CPU baseline and the tests can build them without loading the product library. The
+// values must be bit-identical, so every step is the same double-precision operation in the
+// same order: std::mt19937_64 draws (the C++ standard fixes its output), uniforms as the top
+// 53 bits times 2^-53, exp/log/sin/cos by the same truncated series (not libm, which differs
+// between machines), and one rounding to float at the end.
+
+namespace gen {
+
+constexpr double kLn2 = 0.69314718055994530941723212145818;
+constexpr double kPi = 3.14159265358979323846264338327950;
+
+// e^x as 2^k e^r, r = x - k ln2 in [-ln2/2, ln2/2], e^r by its Taylor series through r^20.
+double exp_series(double x) {
+    const double k = std::floor(x / kLn2 + 0.5);
+    const double r = x - k * kLn2;
+    double term = 1.0, acc = 1.0;
+    for (int i = 1; i <= 20; ++i) {
+        term = term * r / i;
+        acc += term;
+    }
+    return std::ldexp(acc, static_cast<int>(k));
+}
+
+// ln x = e ln2 + ln m with m in [1/sqrt2, sqrt2); ln m = 2 atanh(s), s = (m-1)/(m+1), the
+// atanh series through s^41.
+double log_series(double x) {
+    int e = 0;
+    double m = std::frexp(x, &e);
+    if (m < 0.70710678118654752440) {
+        m *= 2.0;
+        e -= 1;
+    }
+    const double s = (m - 1.0) / (m + 1.0), s2 = s * s;
+    double power = s, acc = 0.0;
+    for (int i = 1; i <= 41; i += 2) {
+        acc += power / i;
+        power *= s2;
+    }
+    return 2.0 * acc + e * kLn2;
+}
+
+// sin x and cos x by their Taylor series (14 terms after the first).
+void sincos_series(double x, double& sn, double& cs) {
+    double ts = x, tc = 1.0;
+    sn = x;
+    cs = 1.0;
+    for (int i = 1; i <= 14; ++i) {
+        ts = -ts * x * x / ((2 * i) * (2 * i + 1));
+        tc = -tc * x * x / ((2 * i - 1) * (2 * i));
+        sn += ts;
+        cs += tc;
+    }
+}
+
+struct Out {
+    std::vector<float> v, alb, em;
+    float cam[10] = {};  // position, target, up, fov
+    void push_tri(const double* a, const double* b, const double* c, const float* albedo, const float* emission) {
+        for (const double* q : {a, b, c})
+            for (int k = 0; k < 3; ++k) v.push_back(static_cast<float>(q[k]));
+        for (int k = 0; k < 3; ++k) {
+            alb.push_back(albedo[k]);
+            em.push_back(emission[k]);
+        }
+    }
+    // corner o and edges u, w: triangles (o, o+u, o+u+w) and (o, o+u+w, o+w), each sum
+    // formed left to right
+    void push_quad(const double* o, const double* u, const double* w, const float* albedo, const float* emission) {
+        double b[3], c[3], d[3];
+        for (int k = 0; k < 3; ++k) {
+            b[k] = o[k] + u[k];
+            c[k] = o[k] + u[k] + w[k];
+            d[k] = o[k] + w[k];
+        }
+        push_tri(o, b, c, albedo, emission);
+        push_tri(o, c, d, albedo, emission);
+    }
+    void camera(float px, float py, float pz, float tx, float ty, float tz, float fov) {
+        const float c[10] = {px, py, pz, tx, ty, tz, 0.f, 1.f, 0.f, fov};
+        std::memcpy(cam, c, sizeof(c));
+    }
+};
+
+void cornell36(Out& o) {
+    const float wht[3] = {0.73f, 0.73f, 0.73f}, red[3] = {0.63f, 0.065f, 0.05f}, grn[3] = {0.14f, 0.45f, 0.09f};
+    const float none[3] = {0.f, 0.f, 0.f}, lamp[3] = {17.f, 12.f, 4.f};
+    const double X[3] = {1, 0, 0}, Y[3] = {0, 1, 0}, Z[3] = {0, 0, 1}, zero[3] = {0, 0, 0};
+    const double ceil_o[3] = {0, 1, 0}, back_o[3] = {0, 0, 1}, right_o[3] = {1, 0, 0};
+    o.push_quad(zero, X, Z, wht, none);      // floor
+    o.push_quad(ceil_o, X, Z, wht, none);    // ceiling
+    o.push_quad(back_o, X, Y, wht, none);    // back wall
+    o.push_quad(right_o, Z, Y, red, none);   // x = 1
+    o.push_quad(zero, Z, Y, grn, none);      // x = 0
+    const double lo[3] = {0.375, 0.999, 0.375}, lu[3] = {0.25, 0, 0}, lw[3] = {0, 0, 0.25};
+    o.push_quad(lo, lu, lw, none, lamp);     // ceiling light
+    auto box = [&](const double base[3], const double size[3], double degrees) {
+        double sn, cs;
+        sincos_series(degrees * kPi / 180.0, sn, cs);
+        double c[8][3];
+        for (int i = 0; i < 8; ++i) {
+            const double lx = (i & 1) ? size[0] * 0.5 : -size[0] * 0.5;
+            const double ly = (i & 4) ? size[1] : 0.0;
+            const double lz = (i & 2) ? size[2] * 0.5 : -size[2] * 0.5;
+            c[i][0] = lx * cs + lz * sn + base[0];
+            c[i][1] = ly + base[1];
+            c[i][2] = -lx * sn + lz * cs + base[2];
+        }
+        const int faces[6][3] = {{4, 5, 6}, {0, 2, 1}, {0, 1, 4}, {3, 2, 7}, {2, 0, 6}, {1, 3, 5}};
+        for (const auto& f : faces) {
+            double u[3], w[3];
+            for (int k = 0; k < 3; ++k) {
+                u[k] = c[f[1]][k] - c[f[0]][k];
+                w[k] = c[f[2]][k] - c[f[0]][k];
+            }
+            o.push_quad(c[f[0]], u, w, wht, none);
+        }
+    };
+    const double b1[3] = {0.66, 0.0, 0.34}, s1[3] = {0.3, 0.3, 0.3};
+    const double b2[3] = {0.34, 0.0, 0.64}, s2[3] = {0.3, 0.6, 0.3};
+    box(b1, s1, -18.0);
+    box(b2, s2, 18.0);
+    o.camera(0.5f, 0.5f, -1.4f, 0.5f, 0.5f, 0.5f, 40.f);
+}
+
+// centres (optional): receives the drawn centre of every triangle (3 doubles each).
+void soup(Out& o, uint32_t n, uint64_t seed, double* centres = nullptr) {
+    std::mt19937_64 eng(seed);
+    auto uniform = [&]() { return static_cast<double>(eng() >> 11) * 0x1p-53; };
+    auto gaussian = [&]() {  // Marsaglia's polar method, first variate
+        double a, b, r;
+        do {
+            a = 2.0 * uniform() - 1.0;
+            b = 2.0 * uniform() - 1.0;
+            r = a * a + b * b;
+        } while (r >= 1.0 || r == 0.0);
+        return a * std::sqrt(-2.0 * log_series(r) / r);
+    };
+    const double mu = log_series(0.005);
+    o.v.assign(9ull * n, 0.f);
+    o.alb.assign(3ull * n, 0.f);
+    o.em.assign(3ull * n, 0.f);
+    for (uint32_t i = 0; i < n; ++i) {
+        const double centre[3] = {uniform(), uniform(), uniform()};
+        if (centres) std::memcpy(centres + 3ull * i, centre, sizeof(centre));
+        for (int k = 0; k < 3; ++k) {
+            double d[3], r2;
+            do {
+                for (double& x : d) x = 2.0 * uniform() - 1.0;
+                r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+            } while (r2 > 1.0 || r2 < 1e-12);
+            const double scale = 1.0 / std::sqrt(r2);
+            const double len = exp_series(mu + 0.5 * gaussian());
+            for (int a = 0; a < 3; ++a) o.v[9ull * i + 3 * k + a] = static_cast<float>(centre[a] + d[a] * scale * len);
+        }
+        for (int k = 0; k < 3; ++k) o.alb[3ull * i + k] = static_cast<float>(0.2 + 0.6 * uniform());
+    }
+    // round(n / 100) emitters drawn without replacement (partial Fisher-Yates), emission
+    // drawn per emitter in ascending index order
+    const uint32_t count = (n + 50) / 100;
+    std::vector<uint32_t> perm(n);
+    for (uint32_t i = 0; i < n; ++i) perm[i] = i;
+    std::vector<uint8_t> lit(n, 0);
+    for (uint32_t k = 0; k < count && k < n; ++k) {
+        const uint32_t j = k + static_cast<uint32_t>(eng() % (n - k));
+        std::swap(perm[k], perm[j]);
+        lit[perm[k]] = 1;
+    }
+    for (uint32_t i = 0; i < n; ++i)
+        if (lit[i])
+            for (int k = 0; k < 3; ++k) o.em[3ull * i + k] = static_cast<float>(1.0 + 9.0 * uniform());
+    o.camera(0.5f, 0.5f, -1.0f, 0.5f, 0.5f, 0.5f, 40.f);
+}
+
+}  // namespace gen
+
+// Builds "cornell36" or "soup:n=N,seed=S" (defaults n = 1000000, seed = 0). On success the
+// three arrays are malloc'd (release with oracle_free) and cam receives position, target, up
+// and fov. Returns 0, or -1 for an unknown spec.
+ORACLE_API int oracle_make_scene(const char* spec, uint32_t* tri_count, float** vertices, float** albedo,
+                                 float** emission, float* cam) {
+    if (!spec || !tri_count || !vertices || !albedo || !emission || !cam) return -1;
+    const std::string sp(spec);
+    gen::Out o;
+    if (sp == "cornell36") {
+        gen::cornell36(o);
+    } else if (sp.rfind("soup", 0) == 0) {
+        auto field = [&](const char* key, uint64_t dflt) {
+            const std::string k = std::string(key) + "=";
+            const size_t at = sp.find(k);
+            return at == std::string::npos ? dflt : std::strtoull(sp.c_str() + at + k.size(), nullptr, 10);
+        };
+        const uint64_t n = field("n", 1000000), seed = field("seed", 0);
+        if (n == 0 || n > (1ull << 26)) return -1;
+        gen::soup(o, static_cast<uint32_t>(n), seed);
+    } else {
+        return -1;
+    }
+    auto dup = [](const std::vector<float>& a) {
+        float* p = static_cast<float*>(std::malloc(sizeof(float) * std::max<size_t>(a.size(), 1)));
+        if (p && !a.empty()) std::memcpy(p, a.data(), sizeof(float) * a.size());
+        return p;
+    };
+    *tri_count = static_cast<uint32_t>(o.v.size() / 9);
+    *vertices = dup(o.v);
+    *albedo = dup(o.alb);
+    *emission = dup(o.em);
+    std::memcpy(cam, o.cam, sizeof(o.cam));
+    return 0;
+}
+
+ORACLE_API void oracle_free(void* p) { std::free(p); }
+
+// The centres the soup generator draws for "soup:n=N,seed=S" (3 doubles per triangle), for
+// tests of its edge-length distribution.
+ORACLE_API int oracle_soup_centres(uint32_t n, uint64_t seed, double* centres) {
+    if (!centres || n == 0) return -1;
+    gen::Out o;
+    gen::soup(o, n, seed, centres);
     return 0;
 }
 

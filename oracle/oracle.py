@@ -59,8 +59,59 @@ def lib() -> C.CDLL:
         L.oracle_hardware_threads.restype = C.c_uint32
         L.oracle_backward.restype = C.c_int
         L.oracle_backward.argtypes = [C.c_uint32, P, P, P, C.POINTER(OracleConfig), P, P, P]
+        L.oracle_make_scene.restype = C.c_int
+        L.oracle_make_scene.argtypes = [C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(C.POINTER(C.c_float)),
+                                        C.POINTER(C.POINTER(C.c_float)), C.POINTER(C.POINTER(C.c_float)), P]
+        L.oracle_free.argtypes = [P]
+        L.oracle_soup_centres.restype = C.c_int
+        L.oracle_soup_centres.argtypes = [C.c_uint32, C.c_uint64, P]
         _lib = L
     return _lib
+
+
+class OracleScene:
+    """A scene built by the oracle's own generators: vertices (n, 9), albedo and emission
+    (n, 3) float32 and the camera (position, target, up, fov), the fields the oracle's render
+    functions read."""
+
+    def __init__(self, vertices, albedo, emission, camera):
+        self.vertices, self.albedo, self.emission, self.camera = vertices, albedo, emission, camera
+
+    @property
+    def tri_count(self) -> int:
+        return int(self.vertices.shape[0])
+
+
+def make_scene(spec: str) -> OracleScene:
+    """The benchmark scenes "cornell36" and "soup:n=N,seed=S" from the oracle's restatement of
+    the library's generators (bit-identical to Q_cuda_make_scene), without the product."""
+    n = C.c_uint32(0)
+    pv, pa, pe = C.POINTER(C.c_float)(), C.POINTER(C.c_float)(), C.POINTER(C.c_float)()
+    cam = np.zeros(10, np.float32)
+    rc = lib().oracle_make_scene(spec.encode(), C.byref(n), C.byref(pv), C.byref(pa), C.byref(pe), cam.ctypes.data)
+    if rc:
+        raise ValueError(f"oracle_make_scene: unknown spec {spec!r}")
+    try:
+        k = int(n.value)
+
+        def arr(p, width):
+            return np.ctypeslib.as_array(p, shape=(k * width,)).reshape(k, width).copy()
+
+        v, a, e = arr(pv, 9), arr(pa, 3), arr(pe, 3)
+    finally:
+        for ptr in (pv, pa, pe):
+            lib().oracle_free(C.cast(ptr, C.c_void_p))
+    camera = {"position": tuple(float(x) for x in cam[0:3]), "target": tuple(float(x) for x in cam[3:6]),
+              "up": tuple(float(x) for x in cam[6:9]), "fov": float(cam[9])}
+    return OracleScene(v, a, e, camera)
+
+
+def soup_centres(n: int, seed: int) -> np.ndarray:
+    """The (n, 3) centres the soup generator draws for "soup:n=N,seed=S"."""
+    out = np.zeros((n, 3), np.float64)
+    if lib().oracle_soup_centres(n, seed, out.ctypes.data):
+        raise ValueError("oracle_soup_centres")
+    return out
 
 
 def _f32(a) -> np.ndarray:
