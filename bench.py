@@ -32,10 +32,13 @@ WIDTH, HEIGHT, SPP, DEPTH = 1920, 1080, 64, 8
 WORKLOAD = "soup-1M 1920x1080 64spp depth8 NEE, LBVH rebuilt every frame"
 TRI_BYTES, RAY_BYTES, HIT_BYTES, SHADOW_BYTES = 48, 32, 16, 48
 NODE_BYTES = {2: 64, 8: 96}  # binary LBVH node / 8-wide record
-# The workload both arms time (the same dict in both JSON lines).
-CONFIG = {"workload": WORKLOAD, "scene": SCENE, "tri_count": 1000000, "width": WIDTH, "height": HEIGHT, "spp": SPP,
-          "max_depth": DEPTH, "lbvh": "built in every step, inside the timed region",
-          "l2": "GPU arm: 256 MiB write before every step, inside the timed region; CPU arm: not applicable"}
+
+
+def workload_config() -> dict:
+    """The workload both arms time (the same dict in both JSON lines)."""
+    return {"workload": WORKLOAD, "scene": SCENE, "tri_count": 1000000, "width": WIDTH, "height": HEIGHT, "spp": SPP,
+            "max_depth": DEPTH, "lbvh": "built in every step, inside the timed region",
+            "l2": "GPU arm: 256 MiB write before every step, inside the timed region; CPU arm: not applicable"}
 
 
 def _peaks() -> tuple[float, str]:
@@ -340,7 +343,7 @@ def run_reference(args) -> None:
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": dict(CONFIG),
+            "config": workload_config(),
             "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": cores, "kind": "port", "sample": desc},
             "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "the reference renderer is a Metal shader (macOS graphics API) and cannot run here; "
@@ -486,7 +489,7 @@ def run_ours(args) -> None:
         line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": frame_ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": dict(CONFIG),
+                "config": workload_config(),
                 "details": {"rays_per_step": rays / args.steps / world, "bvh_ms": st.bvh_ms,
                             "redecided_rays_per_step": st.redecided_rays, "parallelism": f"replicas x{world}",
                             "wave_spp": args.wave_spp, "trace_block": args.trace_block,

@@ -220,7 +220,9 @@ def test_reference_integrator_matches_reference_shader(host, golden):
     aov = host.readback_aov()
     ref = np.array(r["beauty"], np.float64).reshape(h, w, 4)[..., :3]
     err = _rel(aov["beauty"][..., :3].astype(np.float64), ref).max(-1)
-    assert (err <= REL_TOL).mean() >= 0.98, (np.sort(err.ravel())[-8:])
+    print(f"reference integrator vs shader: {int((err > REL_TOL).sum())} of {err.size} pixels over {REL_TOL}, "
+          f"largest errors {np.sort(err.ravel())[-8:]}")
+    assert err.max() <= REL_TOL, (np.sort(err.ravel())[-8:])
     assert np.abs(aov["albedo"][..., :3] - np.array(r["albedo"]).reshape(h, w, 4)[..., :3]).max() < 1e-4
     host.set_options(integrator=0, spp_per_frame=1, max_depth=4)
 
