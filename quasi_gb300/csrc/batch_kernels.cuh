@@ -233,9 +233,13 @@ __global__ void __launch_bounds__(128) k_batch_fixup(const BatchSceneDev* __rest
                 float tmax;
                 int exclude;
                 job.load(i, o, d, tmax, exclude);
-                const RayInv r = make_ray(o, d, s.n_tris ? scene_box_pad(s.nodes) : 0.0f);
-                b = trace_bvh<any, false, false, true>(s.nodes, s.tris, s.tri_in, s.n_tris, r, tmax, exclude, e, cnt,
-                                                       job.exact(i));
+                if (s.wide) {
+                    b = trace_wide_exact<any>(s.wide, s.tris, s.tri_in, s.n_tris, o, d, tmax, exclude, job.exact(i), e);
+                } else {
+                    const RayInv r = make_ray(o, d, s.n_tris ? scene_box_pad(s.nodes) : 0.0f);
+                    b = trace_bvh<any, false, false, true>(s.nodes, s.tris, s.tri_in, s.n_tris, r, tmax, exclude, e,
+                                                           cnt, job.exact(i));
+                }
             } else {
                 b = job.partial(i);
                 redecide<any>(s.tri_in, job.exact(i), en.y, b);

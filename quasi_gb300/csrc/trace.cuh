@@ -407,15 +407,14 @@ __device__ __forceinline__ void trace_persistent(Job& job, const float4* __restr
 // Completes the rays a fast trace kernel deferred: entry k of `list` is (ray i, its
 // undecided candidate). One entry per thread, 32 entries per warp and atomic, so the exact
 // re-decisions run with the lanes in step. A candidate is re-decided against the ray's
-// certain result (job.partial(i)); a ray that met more than one is re-traced whole over the
-// binary LBVH with inline re-decisions. Job supplies load, store, partial(i) and exact(i).
-template <bool ANY, class Job>
-__device__ __forceinline__ void resolve_deferred(Job& job, const float4* __restrict__ nodes,
-                                                 const float4* __restrict__ tris, const float4* __restrict__ tri_in,
-                                                 uint32_t n_tris, const int2* __restrict__ list, int n,
-                                                 int* __restrict__ fetch, uint32_t& err) {
+// certain result (job.partial(i)); a ray that met more than one is re-traced whole with
+// inline re-decisions by `retrace(o, d, tmax, exclude, exact)` (over the 8-wide records or
+// the binary LBVH). Job supplies load, store, partial(i) and exact(i).
+template <bool ANY, class Job, class Retrace>
+__device__ __forceinline__ void resolve_deferred(Job& job, const float4* __restrict__ tri_in,
+                                                 const int2* __restrict__ list, int n, int* __restrict__ fetch,
+                                                 const Retrace& retrace) {
     const int lane = threadIdx.x & 31;
-    TraceCounters cnt;
     while (true) {
         int base = 0;
         if (lane == 0) base = atomicAdd(fetch, 32);
@@ -431,9 +430,7 @@ __device__ __forceinline__ void resolve_deferred(Job& job, const float4* __restr
                 float tmax;
                 int exclude;
                 job.load(i, o, d, tmax, exclude);
-                const RayInv r = make_ray(o, d, n_tris ? scene_box_pad(nodes) : 0.0f);
-                b = trace_bvh<ANY, false, false, true>(nodes, tris, tri_in, n_tris, r, tmax, exclude, err, cnt,
-                                                       job.exact(i));
+                b = retrace(i, o, d, tmax, exclude);
             } else {
                 b = job.partial(i);
                 redecide<ANY>(tri_in, job.exact(i), e.y, b);

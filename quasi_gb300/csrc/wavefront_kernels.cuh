@@ -104,14 +104,23 @@ __global__ void __launch_bounds__(256, trace_min_blocks(MODE)) k_trace_shadow(Sc
 
 // Completes the rays a closest-hit or shadow trace kernel deferred (robust.cuh): re-decides
 // each ray's recorded candidate exactly against its certain result, or re-traces a ray that
-// met more than one, and stores the final results. The list length is read on the device, so
-// the launch needs no host synchronisation; a persistent grid takes 32 entries per warp.
+// met more than one (over the 8-wide records when the scene has them: a third of the
+// binary LBVH's dependent node fetches), and stores the final results. The list length is
+// read on the device, so the launch needs no host synchronisation; a persistent grid takes
+// 32 entries per warp.
 template <class Job>
 __global__ void __launch_bounds__(128) k_fixup(SceneDev s, Job job, int* __restrict__ fetch,
                                                uint32_t* __restrict__ err) {
     constexpr bool any = std::is_same<Job, ShadowJob>::value;
     uint32_t e = 0;
-    resolve_deferred<any>(job, s.nodes, s.tris, s.tri_in, s.n_tris, job.deferred.list, *job.deferred.count, fetch, e);
+    const float pad = s.n_tris && !s.wide ? scene_box_pad(s.nodes) : 0.0f;
+    auto retrace = [&](int i, float3 o, float3 d, float tmax, int exclude) {
+        if (s.wide) return trace_wide_exact<any>(s.wide, s.tris, s.tri_in, s.n_tris, o, d, tmax, exclude, job.exact(i), e);
+        TraceCounters cnt;
+        return trace_bvh<any, false, false, true>(s.nodes, s.tris, s.tri_in, s.n_tris, make_ray(o, d, pad), tmax,
+                                                  exclude, e, cnt, job.exact(i));
+    };
+    resolve_deferred<any>(job, s.tri_in, job.deferred.list, *job.deferred.count, fetch, retrace);
     if (e) atomicOr(err, e);
 }
 

@@ -184,12 +184,15 @@ __device__ __forceinline__ float fmin3(float a, float b, float c) {
 // Tests the triangle of one leaf (one-triangle leaves: a leaf that passed its box test
 // holds exactly one triangle, empty slots never pass); returns true when the traversal ends
 // (an any-hit query answered, or an undecided candidate flagged the ray).
-template <bool ANY, bool STATS>
+// ROBUST: undecided candidates are re-decided exactly (tri_in: original-order vertices, xr:
+// the ray's exact geometry).
+template <bool ANY, bool STATS, bool ROBUST = false, class X = ExactNone>
 __device__ __forceinline__ bool wide_leaf(const float4* __restrict__ tris, const RayInv& r, int ref, int exclude,
-                                          HitBest& b, TraceCounters& cnt) {
+                                          HitBest& b, TraceCounters& cnt, const float4* __restrict__ tri_in = nullptr,
+                                          const X& xr = X{}) {
     static_assert(k_wide_leaf_max == 1, "wide_leaf tests one triangle per leaf");
     if (STATS) ++cnt.tris;
-    return leaf_test<ANY, false>(tris, nullptr, ExactNone{}, r, static_cast<uint32_t>(~ref) >> 2, exclude, b);
+    return leaf_test<ANY, ROBUST>(tris, tri_in, xr, r, static_cast<uint32_t>(~ref) >> 2, exclude, b);
 }
 
 // Traversal state of one ray over the 8-wide records (the stack lives beside it).
@@ -232,9 +235,10 @@ __device__ __forceinline__ int wide_pop(WideRay& q, const Stack& stack) {
 // visit and stacking the other leaves (each loop turn then costs one triangle test, not the
 // busiest lane's count) was measured 7% slower on the 1M soup: the extra stack traffic and
 // loop turns cost more than the divergence they remove.
-template <bool ANY, bool STATS, class Stack>
+template <bool ANY, bool STATS, class Stack, bool ROBUST = false, class X = ExactNone>
 __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, const float4* __restrict__ tris,
-                                           WideRay& q, Stack& stack, uint32_t& err, TraceCounters& cnt) {
+                                           WideRay& q, Stack& stack, uint32_t& err, TraceCounters& cnt,
+                                           const float4* __restrict__ tri_in = nullptr, const X& xr = X{}) {
     if (q.node == k_wide_done) return true;
     if (--q.budget == 0u) {
         err |= k_deverr_traversal;
@@ -308,7 +312,7 @@ __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, cons
     while (lm) {
         const uint32_t s = __ffs(lm) - 1;
         lm &= lm - 1u;
-        if (wide_leaf<ANY, STATS>(tris, r, sel8(refs, s), q.exclude, q.b, cnt)) {
+        if (wide_leaf<ANY, STATS, ROBUST>(tris, r, sel8(refs, s), q.exclude, q.b, cnt, tri_in, xr)) {
             q.node = k_wide_done;
             return true;
         }
@@ -371,6 +375,21 @@ __device__ __forceinline__ TraceResult trace_wide(const float4* __restrict__ wid
     while (!wide_visit<ANY, STATS>(wide, tris, q, stack, err, cnt)) {
     }
     return trace_result(q.b);
+}
+
+// Whole-ray traversal of the 8-wide BVH with exact re-decisions of undecided candidates
+// (xr: the ray's exact geometry, tri_in: original-order vertices); the result is final.
+template <bool ANY, class X>
+__device__ __forceinline__ HitBest trace_wide_exact(const float4* __restrict__ wide, const float4* __restrict__ tris,
+                                                    const float4* __restrict__ tri_in, uint32_t n_tris, float3 o,
+                                                    float3 d, float tmax, int exclude, const X& xr, uint32_t& err) {
+    WideRay q;
+    wide_begin(q, o, d, tmax, exclude, n_tris);
+    WideStack<0> stack;
+    TraceCounters cnt;
+    while (!wide_visit<ANY, false, WideStack<0>, true>(wide, tris, q, stack, err, cnt, tri_in, xr)) {
+    }
+    return q.b;
 }
 
 // Warp-batch persistent traversal of a ray queue over the 8-wide records: a warp takes 32
