@@ -176,8 +176,7 @@ struct ClosestJob {
     __device__ __forceinline__ HitBest partial(int i) const {
         const float4 h = hits[i];
         HitBest b;
-        b.t = h.x;
-        b.dt = 0.0f;
+        b.lo = b.hi = h.x;
         b.prim = __float_as_int(h.y);
         b.undec = k_undec_none;
         return b;
@@ -207,8 +206,7 @@ struct ShadowJob {
     __device__ __forceinline__ void defer(int i, const TraceResult& r) const { deferred.push(i, r.undec); }
     __device__ __forceinline__ HitBest partial(int i) const {
         HitBest b;
-        b.t = sq[3 * i + 1].w;
-        b.dt = 0.0f;
+        b.lo = b.hi = sq[3 * i + 1].w;
         b.prim = -1;
         b.undec = k_undec_none;
         return b;
@@ -381,7 +379,7 @@ __device__ __forceinline__ float3 trace_path(const FrameParams& f, const SceneDe
                                                                 __int_as_float(0x7f800000), exclude, err, cnt,
                                                                 ExactRegs{ro, rd});
         const int prim = hb.prim;
-        const float t = hb.t;
+        const float t = hit_t(hb);
         if (prim < 0) {
             sig = sig_mix(sig, k_sig_miss);
             break;

@@ -30,10 +30,12 @@
 //   |dUd| <= 1.74 u B sigma,  |dVd| <= 2 u A sigma,  |dDet| <= 22.7 u A B,
 //   |dTd| <= 2 u A B sigma
 // where Ud = (o - v0).p, Vd = d.q, Td = E2.q, det = E1.p, p = d x E2, q = (o - v0) x E1.
-// For |u|, |v| <= 4 the computed u = Ud/det, v = Vd/det and w = 1 - u - v are each within
-//   M = u (sigma (1.74 B + 2 A) + 363.2 A B) / |det| + 34 u
-// of their exact values, and t = Td/det within
-//   dt = u A B (2 sigma + 45.4 |t|) / |det| + 2 u |t|.
+// 1/det is the hardware reciprocal approximation (relative error <= 2^-23 = 2u), so u, v and
+// t carry 3u of relative rounding from their normalisation. For |u|, |v| <= 4 the computed
+// u = Ud/det, v = Vd/det and w = 1 - u - v are each within
+//   M = u (sigma (1.74 B + 2 A) + 363.2 A B) / |det| + 48 u
+// of their exact values (48 u >= 5 u (|u| + |v|) + 2 u), and t = Td/det within
+//   dt = u A B (2 sigma + 45.4 |t|) / |det| + 4 u |t|.
 // A coordinate with |u| or |v| > 4 is a certain miss whenever M < 1 (the relative error of
 // det is then below 1/16). The per-triangle factors K1 = 1.01 u (1.74 B + 2 A) and
 // K2 = 1.01 * 363.2 u A B are stored with the leaf triangles (e1.w, e2.w).
@@ -48,7 +50,7 @@ constexpr float k_ulp = 0x1p-24f;
 // Per-triangle error factors (written with the leaf triangles by the LBVH build).
 __host__ __device__ __forceinline__ float robust_k1(float a, float b) { return 1.01f * k_ulp * (1.74f * b + 2.0f * a); }
 __host__ __device__ __forceinline__ float robust_k2(float a, float b) { return 1.01f * 363.2f * k_ulp * a * b; }
-// dt = K2 (sigma / 181.6 + |t| / 8) / |det| + 2 u |t| (from u A B = K2 / (1.01 * 363.2)).
+// dt = K2 (sigma / 181.6 + |t| / 8) / |det| + 4 u |t| (from u A B = K2 / (1.01 * 363.2)).
 constexpr float k_dt_sigma = 1.0f / 181.6f;
 constexpr float k_dt_t = 0.125f;
 
@@ -64,6 +66,21 @@ constexpr float k_box_pad_rel = 0x1p-16f;
 constexpr float k_seg_end_hi = 0.99989998340606689453125f;  // float nearest 1 - 1e-4
 constexpr float k_seg_end_lo = 1.6593933338526767e-08f;     // (1 - 1e-4) - hi, rounded
 
+// Reciprocal by the hardware approximation (rcp.approx.ftz.f32: relative error <= 2^-23;
+// subnormal inputs flush to zero and give inf, which the error bound turns into undecided).
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Largest absolute component.
+__device__ __forceinline__ float max_abs3(float3 v) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(fabsf(v.x)), "f"(fabsf(v.y)), "f"(fabsf(v.z)));
+    return r;
+}
+
 // Outcome of one FP32 triangle test.
 enum : int { k_tri_miss = 0, k_tri_hit = 1, k_tri_undecided = 2 };
 
@@ -76,7 +93,7 @@ __device__ __forceinline__ int tri_classify(float3 o, float3 d, float4 a, float4
     const float3 E1 = xyz(e1), E2 = xyz(e2);
     const float3 p = cross(d, E2);
     const float det = dot(E1, p);
-    const float inv = 1.0f / det;  // det == 0 gives inf/nan: the bound is then inf/nan, undecided
+    const float inv = rcp_approx(det);  // det == 0 gives inf/nan: the bound is then inf/nan, undecided
     const float3 tv = o - xyz(a);
     const float u = dot(tv, p) * inv;
     const float3 q = cross(tv, E1);
@@ -84,11 +101,10 @@ __device__ __forceinline__ int tri_classify(float3 o, float3 d, float4 a, float4
     t = dot(E2, q) * inv;
     const float w = 1.0f - u - v;
     const float ainv = fabsf(inv);
-    const float sigma = fmaf(ANY ? 13.0f : 8.0f, fmaxf(fabsf(tv.x), fmaxf(fabsf(tv.y), fabsf(tv.z))),
-                             fmaxf(fabsf(o.x), fmaxf(fabsf(o.y), fabsf(o.z))));
-    const float m = fmaf(fmaf(e1.w, sigma, e2.w), ainv, 34.0f * k_ulp);
+    const float sigma = fmaf(ANY ? 13.0f : 8.0f, max_abs3(tv), max_abs3(o));
+    const float m = fmaf(fmaf(e1.w, sigma, e2.w), ainv, 48.0f * k_ulp);
     const float at = fabsf(t);
-    dt = fmaf(e2.w * ainv, fmaf(at, k_dt_t, sigma * k_dt_sigma), 2.0f * k_ulp * at);
+    dt = fmaf(e2.w * ainv, fmaf(at, k_dt_t, sigma * k_dt_sigma), 4.0f * k_ulp * at);
     const float mn = fminf(u, fminf(v, w));
     if (mn > m && t > dt) return k_tri_hit;
     if ((mn < -m && m < 1.0f) || (mn > m && t < -dt)) return k_tri_miss;
@@ -152,11 +168,13 @@ constexpr int k_undec_many = -2;
 
 // Closest-hit state of one ray (or the any-hit state of a shadow segment).
 struct HitBest {
-    float t;     // closest certain hit so far (t_max before any); box tests cull beyond t + dt
-    float dt;    // bound on |t - exact t| of the closest hit
-    int prim;    // original index, or -1
-    int undec;   // fast traversal: the undecided candidate met (orig), k_undec_none or _many
+    float lo, hi;  // the exact t of the closest certain hit so far lies in [lo, hi] (t_max's
+                   // interval before any); box tests cull beyond hi
+    int prim;      // original index, or -1
+    int undec;     // fast traversal: the undecided candidate met (orig), k_undec_none or _many
 };
+// The closest hit's t (the middle of its interval).
+__device__ __forceinline__ float hit_t(const HitBest& b) { return 0.5f * (b.lo + b.hi); }
 
 // Re-decides candidate `orig` (vertices from the original-order triangle array) exactly and
 // updates `b`. Returns true when an any-hit query is answered (the segment is blocked).
@@ -186,8 +204,9 @@ __device__ __noinline__ bool redecide(const float4* __restrict__ tri_in, const X
         }
     }
     const float tf = ff_f(t);
-    b.t = tf;
-    b.dt = 2.0f * k_ulp * fabsf(tf);
+    const float dtf = 2.0f * k_ulp * fabsf(tf);
+    b.lo = tf - dtf;
+    b.hi = tf + dtf;
     b.prim = orig;
     return false;
 }

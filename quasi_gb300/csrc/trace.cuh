@@ -85,9 +85,10 @@ __device__ __forceinline__ float box_entry(const RayInv& r, float lox, float hix
 // Start of a closest-hit (t_max = inf) or any-hit (t_max of the segment) query.
 __device__ __forceinline__ HitBest hit_begin(float tmax) {
     HitBest b;
-    b.t = tmax;
     // t_max of a shadow segment is FP32 (its length times 1 - 1e-4, a few roundings)
-    b.dt = tmax < __int_as_float(0x7f800000) ? 8.0f * k_ulp * tmax : 0.0f;
+    const float dt = tmax < __int_as_float(0x7f800000) ? 8.0f * k_ulp * tmax : 0.0f;
+    b.lo = tmax - dt;
+    b.hi = tmax + dt;
     b.prim = -1;
     b.undec = k_undec_none;
     return b;
@@ -112,14 +113,14 @@ __device__ __forceinline__ bool leaf_test(const float4* __restrict__ tris, const
     const int c = tri_classify<ANY>(r.o, r.d, a, e1, e2, t, dt);
     if (c == k_tri_miss) return false;
     if (c == k_tri_hit) {
-        if (t + dt < b.t - b.dt) {  // certainly closer than the closest so far (inside t_max)
-            b.t = t;
-            b.dt = dt;
+        if (t + dt < b.lo) {  // certainly closer than the closest so far (inside t_max)
+            b.lo = t - dt;
+            b.hi = t + dt;
             b.prim = orig;
             if (ANY) b.undec = k_undec_none;  // a certain occluder answers the query
             return ANY;
         }
-        if (t - dt > b.t + b.dt) return false;  // certainly farther
+        if (t - dt > b.hi) return false;  // certainly farther
     }
     if constexpr (ROBUST) {
         return redecide<ANY>(tri_in, xr, orig, b);
@@ -151,7 +152,7 @@ struct TraceResult {
     int prim;
     int undec;
 };
-__device__ __forceinline__ TraceResult trace_result(const HitBest& b) { return TraceResult{b.t, b.prim, b.undec}; }
+__device__ __forceinline__ TraceResult trace_result(const HitBest& b) { return TraceResult{hit_t(b), b.prim, b.undec}; }
 
 // Per-ray traversal state of the resumable binary traversal (the stack lives beside it).
 struct TraceState {
@@ -187,7 +188,7 @@ __device__ __forceinline__ bool trace_step(const float4* __restrict__ nodes, con
     const float4 n1 = __ldg(&nodes[4 * s.node + 1]);
     const float4 n2 = __ldg(&nodes[4 * s.node + 2]);
     const float4 n3 = __ldg(&nodes[4 * s.node + 3]);
-    const float tcull = s.b.t + s.b.dt;
+    const float tcull = s.b.hi;
     const float t0 = box_entry(s.r, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, tcull);
     const float t1 = box_entry(s.r, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, tcull);
     const int c0 = __float_as_int(n3.x);
@@ -196,7 +197,7 @@ __device__ __forceinline__ bool trace_step(const float4* __restrict__ nodes, con
     for (int k = 0; k < 2; ++k) {
         const int c = k == 0 ? c0 : c1;
         const float tb = k == 0 ? t0 : t1;
-        if (c < 0 && tb < s.b.t + s.b.dt) {
+        if (c < 0 && tb < s.b.hi) {
             if (STATS) ++cnt.tris;
             if (leaf_test<ANY, false>(tris, nullptr, ExactNone{}, s.r, ~c, s.exclude, s.b)) {
                 s.node = -1;
@@ -204,7 +205,7 @@ __device__ __forceinline__ bool trace_step(const float4* __restrict__ nodes, con
             }
         }
     }
-    const float tc = s.b.t + s.b.dt;
+    const float tc = s.b.hi;
     const bool h0 = c0 >= 0 && t0 < tc;
     const bool h1 = c1 >= 0 && t1 < tc;
     if (h0 && h1) {
@@ -272,7 +273,7 @@ __device__ __forceinline__ HitBest trace_bvh(const float4* __restrict__ nodes, c
             n2 = __ldg(&nodes[4 * node + 2]);
             n3 = __ldg(&nodes[4 * node + 3]);
         }
-        const float tcull = b.t + b.dt;
+        const float tcull = b.hi;
         float t0 = box_entry(r, n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, tcull);
         float t1 = box_entry(r, n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, tcull);
         int c0 = __float_as_int(n3.x);
@@ -282,13 +283,13 @@ __device__ __forceinline__ HitBest trace_bvh(const float4* __restrict__ nodes, c
         for (int k = 0; k < 2; ++k) {
             const int c = k == 0 ? c0 : c1;
             const float tb = k == 0 ? t0 : t1;
-            if (!ended && c < 0 && tb < b.t + b.dt) {
+            if (!ended && c < 0 && tb < b.hi) {
                 if (STATS) ++cnt.tris;
                 ended = leaf_test<ANY, ROBUST>(tris, tri_in, xr, r, ~c, exclude, b);
             }
         }
         if (ended) break;
-        const float tc = b.t + b.dt;
+        const float tc = b.hi;
         const bool h0 = c0 >= 0 && t0 < tc;
         const bool h1 = c1 >= 0 && t1 < tc;
         if (h0 && h1) {

@@ -221,7 +221,7 @@ __device__ __forceinline__ void wide_begin(WideRay& q, float3 o, float3 d, float
 // or k_wide_done.
 template <class Stack>
 __device__ __forceinline__ int wide_pop(WideRay& q, const Stack& stack) {
-    const float tcull = q.b.t + q.b.dt;
+    const float tcull = q.b.hi;
     while (q.sp > 0) {
         const int2 e = stack.get(--q.sp);
         if (__int_as_float(e.y) < tcull) return e.x;
@@ -273,7 +273,7 @@ __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, cons
     // any-hit rays: the internal child whose box covers the longest stretch of the segment
     float best_ov = -1.0f;
     uint32_t best_slot = 0;
-    const float tcull = q.b.t + q.b.dt;
+    const float tcull = q.b.hi;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         const uint32_t nxw = k < 4 ? nx0 : nx1, fxw = k < 4 ? fx0 : fx1;
@@ -344,7 +344,7 @@ __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, cons
         im &= im - 1u;
         const uint32_t s = p ^ q.oct;
         const float t = sel8(tn, s);
-        if (t >= q.b.t + q.b.dt) continue;
+        if (t >= q.b.hi) continue;
         const int ref = sel8(refs, s);
         if (im) {
             if (q.sp >= k_wide_stack) {
