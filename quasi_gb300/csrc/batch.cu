@@ -41,7 +41,7 @@ BatchRenderer::~BatchRenderer() {
     drop_graphs();
     for (auto& b : bvh_) b->release();
     for (DeviceBuffer* b : {&tri_in_, &albedo_, &emission_, &emitters_, &accum_, &comp_, &aov_a_, &aov_n_, &table_,
-                            &items_, &queue_[0], &queue_[1], &hits_, &shadow_, &beta_, &lpath_, &pa_, &pn_, &ray_ff_, &shadow_ff_, &defer_,
+                            &items_, &queue_[0], &queue_[1], &hits_, &shadow_, &beta_, &lpath_, &pa_, &pn_, &ray_ff_, &defer_,
                             &meta_, &counters_, &adj_counters_, &stats_dev_, &err_dev_, &grad_image_, &grad_albedo_,
                             &grad_emission_})
         b->release();
@@ -222,10 +222,9 @@ int BatchRenderer::upload_table() {
 // Cuts every scene's frame (min(spp, spp_cap) samples) into items of whole sample planes and
 // packs them into waves of at most W path slots, scene after scene.
 int BatchRenderer::plan(uint32_t spp_cap) {
-    // per path slot: two ray queues (2 x 32), hit 16, shadow ray 48, beta, radiance and two
-    // AOVs (4 x 16), double-float ray 48, (scene, local path) 8, exact shadow segment 48,
-    // fixup list entry 8
-    constexpr size_t bytes_per_path = 304;
+    // per path slot: two ray queues (2 x 32), hit 16, shadow ray 64, beta, radiance and two
+    // AOVs (4 x 16), double-float ray 48, (scene, local path) 8, fixup list entry 8
+    constexpr size_t bytes_per_path = 272;
     uint32_t W = opt_.wave_paths ? opt_.wave_paths
                                  : static_cast<uint32_t>(wave_paths_fitting(k_default_wave_paths, bytes_per_path,
                                                                             size_t(wave_capacity_) * bytes_per_path));
@@ -274,13 +273,12 @@ int BatchRenderer::ensure_buffers() {
         B_TRY(queue_[0].reserve(sizeof(float4) * 2ull * paths), "queue");
         B_TRY(queue_[1].reserve(sizeof(float4) * 2ull * paths), "queue");
         B_TRY(hits_.reserve(sizeof(float4) * paths), "hits");
-        B_TRY(shadow_.reserve(sizeof(float4) * 3ull * paths), "shadow");
+        B_TRY(shadow_.reserve(sizeof(float4) * 4ull * paths), "shadow");
         B_TRY(beta_.reserve(sizeof(float4) * paths), "beta");
         B_TRY(lpath_.reserve(sizeof(float4) * paths), "lpath");
         B_TRY(pa_.reserve(sizeof(float4) * paths), "aov");
         B_TRY(pn_.reserve(sizeof(float4) * paths), "aov");
         B_TRY(ray_ff_.reserve(sizeof(float4) * 3ull * paths), "ray_ff");
-        B_TRY(shadow_ff_.reserve(sizeof(float4) * 3ull * paths), "shadow_ff");
         B_TRY(defer_.reserve(sizeof(int2) * paths), "defer");
         B_TRY(meta_.reserve(sizeof(uint2) * paths), "meta");
         wave_capacity_ = paths;
@@ -326,7 +324,7 @@ int BatchRenderer::record_frame(cudaStream_t s, uint32_t& launches) {
     const BatchSceneDev* table = table_.as<BatchSceneDev>();
     const BatchItem* items = items_.as<BatchItem>();
     PathDev pd{beta_.as<float4>(), lpath_.as<float4>(), pa_.as<float4>(), pn_.as<float4>(), ray_ff_.as<float4>(),
-               nullptr, shadow_ff_.as<float4>()};
+               nullptr};
     uint2* meta = meta_.as<uint2>();
     uint32_t* err = err_dev_.as<uint32_t>();
     unsigned long long* st = stats_dev_.as<unsigned long long>();

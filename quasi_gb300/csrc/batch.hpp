@@ -88,7 +88,7 @@ private:
     DeviceBuffer items_;    // BatchItem per item
     // wave buffers
     DeviceBuffer queue_[2], hits_, shadow_, beta_, lpath_, pa_, pn_, ray_ff_, meta_;
-    DeviceBuffer shadow_ff_, defer_;  // exact shadow segments; rays deferred to the fixup kernels
+    DeviceBuffer defer_;  // rays deferred to the fixup kernels
     uint32_t wave_capacity_ = 0;
     DeviceBuffer counters_, adj_counters_, stats_dev_, err_dev_;
     // adjoint staging (the adjoint graph reads and writes these fixed buffers)

@@ -65,8 +65,6 @@ struct PathDev {
     float4* aov_n;      // first-hit remapped normal
     float4* ray_ff;     // 3 float4 per path: the double-float ray of the path's next segment
     uint32_t* sig;      // path signatures (record mode) or null
-    float4* shadow_ff;  // 3 float4 per path: the exact shadow segment of the current vertex
-                        // (start, end - start in double-float), for exact re-decisions
 };
 
 // Rays a fast trace kernel could not decide for certain (robust.cuh): entries (ray index,
@@ -193,35 +191,53 @@ struct ClosestJob {
     }
 };
 
-// Shadow queue: sq[3i] = (origin, path id), sq[3i+1] = (direction, t_max), sq[3i+2] =
-// (contribution); an unoccluded ray adds its contribution to the path's radiance. The exact
-// segment of path pid is p.shadow_ff[3 pid]. A deferred ray found no certain occluder (it
-// would have stopped there), so its certain result is "unoccluded".
+// The exact segment of a shadow ray, for re-decisions: its start (the lifted light sample,
+// double-float: the hi parts are the queue's FP32 origin, the lo parts ride in the queue
+// entry) and its end, the lifted shading point, which is the origin of the path's stored
+// double-float ray (shading writes it whether or not the path continues).
+struct ExactSeg {
+    ff3 start;
+    const float4* ray;
+    __device__ __forceinline__ void get(ff3& o, ff3& d) const {
+        ff3 end, unused;
+        ff_ray_load(ray, end, unused);
+        o = start;
+        d = ff3_sub(end, start);
+    }
+};
+
+// Shadow queue, 4 float4 per ray: sq[4i] = (origin, path id), sq[4i+1] = (direction, t_max),
+// sq[4i+2] = (contribution, origin lo.x), sq[4i+3] = (origin lo.y, origin lo.z, -, -); an
+// unoccluded ray adds its contribution to the path's radiance. A deferred ray found no
+// certain occluder (it would have stopped there), so its certain result is "unoccluded".
 struct ShadowJob {
     const float4* __restrict__ sq;
     PathDev p;
     DeferList deferred;
-    __device__ __forceinline__ int pid(int i) const { return __float_as_int(sq[3 * i].w); }
-    __device__ __forceinline__ ExactPtr exact(int i) const { return ExactPtr{p.shadow_ff + 3ull * pid(i)}; }
+    __device__ __forceinline__ int pid(int i) const { return __float_as_int(sq[4 * i].w); }
+    __device__ __forceinline__ ExactSeg exact(int i) const {
+        const float4 a = sq[4 * i], c = sq[4 * i + 2], e = sq[4 * i + 3];
+        return ExactSeg{ff3{ff{a.x, c.w}, ff{a.y, e.x}, ff{a.z, e.y}}, p.ray_ff + 3ull * __float_as_int(a.w)};
+    }
     __device__ __forceinline__ void defer(int i, const TraceResult& r) const { deferred.push(i, r.undec); }
     __device__ __forceinline__ HitBest partial(int i) const {
         HitBest b;
-        b.lo = b.hi = sq[3 * i + 1].w;
+        b.lo = b.hi = sq[4 * i + 1].w;
         b.prim = -1;
         b.undec = k_undec_none;
         return b;
     }
     __device__ __forceinline__ void load(int i, float3& o, float3& d, float& tmax, int& exclude) const {
-        const float4 r0 = sq[3 * i], r1 = sq[3 * i + 1];
+        const float4 r0 = sq[4 * i], r1 = sq[4 * i + 1];
         o = xyz(r0);
         d = xyz(r1);
         tmax = r1.w;
         exclude = -1;
     }
     __device__ __forceinline__ void store(int i, const TraceResult& s) const {
-        const int pid = __float_as_int(sq[3 * i].w);
+        const int pid = __float_as_int(sq[4 * i].w);
         if (s.prim < 0) {
-            const float4 c = sq[3 * i + 2];
+            const float4 c = sq[4 * i + 2];
             float4 L = p.lpath[pid];
             L.x += c.x;
             L.y += c.y;
@@ -245,6 +261,7 @@ struct HitShade {
     bool next;              // enqueue the continuation ray (norg, nd)
     float3 contrib;
     float3 so, sd;
+    float3 so_lo;           // lo parts of the exact (double-float) shadow ray origin
     float stmax;
     float3 norg, nd;
 };
@@ -276,9 +293,9 @@ __device__ __forceinline__ void shade_hit(const FrameParams& f, const SceneDev& 
     }
     o.shadow = v.nee;
     if (v.nee) {
-        ff_ray_store(&p.shadow_ff[3ull * pid], v.seg_o, v.seg_d);
         o.contrib = beta * alb * xyz(__ldg(&s.emission[v.light])) * v.g;
         o.so = v.so;
+        o.so_lo = mk3(v.seg_o.x.lo, v.seg_o.y.lo, v.seg_o.z.lo);
         o.sd = v.sd;
         o.stmax = v.stmax;
     } else {
@@ -291,6 +308,9 @@ __device__ __forceinline__ void shade_hit(const FrameParams& f, const SceneDev& 
         ff_ray_store(&p.ray_ff[3ull * pid], v.org, v.dir);
         o.norg = ff3_f(v.org);
         o.nd = ff3_f(v.dir);
+    } else if (v.nee) {
+        // the shadow segment's end, for its exact re-decision (ExactSeg)
+        ff_ray_store(&p.ray_ff[3ull * pid], v.org, ff3{});
     }
 }
 
@@ -302,9 +322,10 @@ __device__ __forceinline__ void enqueue_shaded(bool active, int pid, int prim, c
     const bool want_next = active && o.next && next_count != nullptr;
     const int ps = warp_append(0xffffffffu, want_shadow, shadow_count);
     if (want_shadow) {
-        shadow_q[3 * ps] = make_float4(o.so.x, o.so.y, o.so.z, __int_as_float(pid));
-        shadow_q[3 * ps + 1] = make_float4(o.sd.x, o.sd.y, o.sd.z, o.stmax);
-        shadow_q[3 * ps + 2] = make_float4(o.contrib.x, o.contrib.y, o.contrib.z, 0.f);
+        shadow_q[4 * ps] = make_float4(o.so.x, o.so.y, o.so.z, __int_as_float(pid));
+        shadow_q[4 * ps + 1] = make_float4(o.sd.x, o.sd.y, o.sd.z, o.stmax);
+        shadow_q[4 * ps + 2] = make_float4(o.contrib.x, o.contrib.y, o.contrib.z, o.so_lo.x);
+        shadow_q[4 * ps + 3] = make_float4(o.so_lo.y, o.so_lo.z, 0.f, 0.f);
     }
     const int pn = warp_append(0xffffffffu, want_next, next_count);
     if (want_next) {

@@ -134,10 +134,9 @@ private:
     // wavefront
     DeviceBuffer queue_[2];       // 2 float4 per ray
     DeviceBuffer hits_;           // float4 per ray: t, prim, u, v
-    DeviceBuffer shadow_;         // 3 float4 per shadow ray
+    DeviceBuffer shadow_;         // 4 float4 per shadow ray
     DeviceBuffer beta_, lpath_, aov_a_, aov_n_, sig_;
     DeviceBuffer ray_ff_;         // 3 float4 per path: double-float ray of the next segment
-    DeviceBuffer shadow_ff_;      // 3 float4 per path: exact shadow segment of the current vertex
     DeviceBuffer defer_;          // int2 per path slot: rays deferred to the fixup kernels
     DeviceBuffer counters_;       // int counters of the current frame
     DeviceBuffer stats_dev_;      // uint64 stats

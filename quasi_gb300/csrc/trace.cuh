@@ -24,8 +24,6 @@
 namespace quasi {
 
 constexpr int k_stack_size = 64;
-// Box tests widen t_max by a few ulps so FP32 rounding never culls a box the ray touches.
-constexpr float k_box_pad = 1.0000004f;
 // Persistent kernels refill a warp once at least this many of its lanes are idle (default).
 constexpr int k_refill_lanes = 32;
 // Node visits per lane between two refill checks (default).
@@ -79,7 +77,9 @@ __device__ __forceinline__ float box_entry(const RayInv& r, float lox, float hix
     const float tz0 = fmaf(loz, r.inv.z, -r.oinv_lo.z), tz1 = fmaf(hiz, r.inv.z, -r.oinv_hi.z);
     const float tmin = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), 0.0f));
     const float tfar = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
-    return tmin <= tfar * k_box_pad ? tmin : __int_as_float(0x7f800000);
+    // no relative slack is needed: where the exact ray touches the unpadded box its padded
+    // slabs overlap by 2 pad, far above the planes' rounding (robust.cuh)
+    return tmin <= tfar ? tmin : __int_as_float(0x7f800000);
 }
 
 // Start of a closest-hit (t_max = inf) or any-hit (t_max of the segment) query.

@@ -74,7 +74,7 @@ Renderer::~Renderer() {
     bvh_.release();
     for (DeviceBuffer* b : {&raw_vertices_, &tri_in_, &albedo_, &emission_, &emitters_, &quads_, &accum_, &comp_,
                             &aov_albedo_, &aov_normal_, &record_rad_, &record_sig_, &queue_[0], &queue_[1], &hits_,
-                            &shadow_, &beta_, &lpath_, &aov_a_, &aov_n_, &sig_, &ray_ff_, &shadow_ff_, &defer_,
+                            &shadow_, &beta_, &lpath_, &aov_a_, &aov_n_, &sig_, &ray_ff_, &defer_,
                             &counters_, &stats_dev_, &err_dev_})
         b->release();
     if (counters_host_) cudaFreeHost(counters_host_);
@@ -247,24 +247,23 @@ int Renderer::ensure_frame_buffers(uint32_t w, uint32_t h) {
     return reset();
 }
 
-// Bytes of wave state per path slot: two ray queues (2 x 32), hit 16, shadow ray 48, beta,
-// radiance and two AOVs (4 x 16), signature 4, double-float ray 48, exact shadow segment 48,
-// fixup list entry 8.
-constexpr size_t k_wave_bytes_per_path = 300;
+// Bytes of wave state per path slot: two ray queues (2 x 32), hit 16, shadow ray 64 (with the
+// lo parts of its exact origin), beta, radiance and two AOVs (4 x 16), signature 4,
+// double-float ray 48, fixup list entry 8.
+constexpr size_t k_wave_bytes_per_path = 268;
 
 int Renderer::ensure_wave_buffers(uint32_t paths) {
     if (paths <= wave_capacity_) return QUASI_OK;
     R_TRY(queue_[0].reserve(sizeof(float4) * 2ull * paths), "queue");
     R_TRY(queue_[1].reserve(sizeof(float4) * 2ull * paths), "queue");
     R_TRY(hits_.reserve(sizeof(float4) * paths), "hits");
-    R_TRY(shadow_.reserve(sizeof(float4) * 3ull * paths), "shadow");
+    R_TRY(shadow_.reserve(sizeof(float4) * 4ull * paths), "shadow");
     R_TRY(beta_.reserve(sizeof(float4) * paths), "beta");
     R_TRY(lpath_.reserve(sizeof(float4) * paths), "lpath");
     R_TRY(aov_a_.reserve(sizeof(float4) * paths), "aov");
     R_TRY(aov_n_.reserve(sizeof(float4) * paths), "aov");
     R_TRY(sig_.reserve(sizeof(uint32_t) * paths), "sig");
     R_TRY(ray_ff_.reserve(sizeof(float4) * 3ull * paths), "ray_ff");
-    R_TRY(shadow_ff_.reserve(sizeof(float4) * 3ull * paths), "shadow_ff");
     R_TRY(defer_.reserve(sizeof(int2) * paths), "defer");
     wave_capacity_ = paths;
     return QUASI_OK;
@@ -372,8 +371,7 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
                 bv.tri_nrm};
     const size_t tree_smem = sizeof(float4) * 4 * static_cast<size_t>(sd.tree_n);
     PathDev pd{beta_.as<float4>(),  lpath_.as<float4>(), aov_a_.as<float4>(),
-               aov_n_.as<float4>(), ray_ff_.as<float4>(), opt_.record_samples ? sig_.as<uint32_t>() : nullptr,
-               shadow_ff_.as<float4>()};
+               aov_n_.as<float4>(), ray_ff_.as<float4>(), opt_.record_samples ? sig_.as<uint32_t>() : nullptr};
     FrameParams f{};
     f.cam = make_camera_basis(camera_, width_, height_);
     f.width = width_;
@@ -524,8 +522,7 @@ int Renderer::render_megakernel(cudaStream_t s, uint32_t spp) {
     const SceneDev sd = Renderer_scene_dev(bvh_.view(), tri_in_, albedo_, emission_, emitters_, n_tris_, n_emit_,
                                            opt_.bvh_width);
     PathDev pd{beta_.as<float4>(),  lpath_.as<float4>(), aov_a_.as<float4>(),
-               aov_n_.as<float4>(), ray_ff_.as<float4>(), opt_.record_samples ? sig_.as<uint32_t>() : nullptr,
-               shadow_ff_.as<float4>()};
+               aov_n_.as<float4>(), ray_ff_.as<float4>(), opt_.record_samples ? sig_.as<uint32_t>() : nullptr};
     FrameParams f = frame_params(spp, slots, tiles_x);
     int occ = 0;
     auto kern = opt_.collect_stats ? k_megakernel<true> : k_megakernel<false>;

@@ -293,7 +293,8 @@ __device__ __forceinline__ bool wide_visit(const float4* __restrict__ wide, cons
         const float tnear = fmax3(tnx, tny, fmaxf(tnz, 0.0f));
         const float tfar = fmin3(tfx, tfy, fminf(tfz, tcull));
         tn[k] = tnear;
-        const bool h = tnear <= tfar * k_box_pad;
+        // the decoded boxes carry the scene's spatial padding: no relative slack needed
+        const bool h = tnear <= tfar;
         hit |= (h ? 1u : 0u) << k;
         if (ANY) {
             const float ov = tfar - tnear;
