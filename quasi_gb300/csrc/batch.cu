@@ -368,7 +368,7 @@ int BatchRenderer::record_frame(cudaStream_t s, uint32_t& launches) {
                 int* c_shadow = cnt + D + (k - 1);
                 int* f_cur = cnt + 2 * D + (k - 1);
                 int* f_shadow = cnt + 3 * D + (k - 1);
-                const ClosestJob cjob{qcur, hits_.as<float4>(), ray_ff_.as<float4>(),
+                const ClosestJob cjob{qcur, hits_.as<float4>(), ray_ff_.as<float4>(), lpath_.as<float4>(),
                                       DeferList{defer_.as<int2>(), cnt + 4 * D + (k - 1)}};
                 const ShadowJob sjob{shadow_.as<float4>(), pd, DeferList{defer_.as<int2>(), cnt + 5 * D + (k - 1)}};
                 B_TRY(QUASI_LAUNCH(prof_, "batch_trace_closest", s,

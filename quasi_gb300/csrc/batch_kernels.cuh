@@ -76,7 +76,8 @@ __global__ void __launch_bounds__(256) k_batch_camera(const BatchSceneDev* __res
     const uint32_t local = item_local(it, gid);
     meta[gid] = make_uint2(it.scene, local);
     float3 o = mk3(0.f, 0.f, 0.f), d = o;
-    const bool valid = begin_path(scenes[it.scene].f, p, gid, local, o, d);
+    const BatchSceneDev& b = scenes[it.scene];
+    const bool valid = begin_path(b.f, p, gid, local, b.s.nodes, b.s.n_tris, o, d);
     const int pos = warp_append(0xffffffffu, valid, q_count);
     if (valid) {
         q[2 * pos] = make_float4(o.x, o.y, o.z, __int_as_float(static_cast<int>(gid)));

@@ -135,10 +135,35 @@ __device__ __forceinline__ void camera_ray_ff(const FrameParams& f, uint32_t x, 
     o = ff3v(f.cam.origin);
 }
 
+// Distance along the ray (o, d) to just before where it enters the scene's bounding box (the
+// union of the binary LBVH root's child boxes), or 0 when it starts inside or misses it.
+__device__ __forceinline__ float scene_entry(const float4* __restrict__ nodes, float3 o, float3 d) {
+    const float4 n0 = __ldg(&nodes[0]), n1 = __ldg(&nodes[1]), n2 = __ldg(&nodes[2]);
+    const float lo[3] = {fminf(n0.x, n1.x), fminf(n0.z, n1.z), fminf(n2.x, n2.z)};
+    const float hi[3] = {fmaxf(n0.y, n1.y), fmaxf(n0.w, n1.w), fmaxf(n2.y, n2.w)};
+    const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+    float t0 = 0.0f, t1 = __int_as_float(0x7f800000);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float inv = 1.0f / dd[a];
+        float ta = (lo[a] - oo[a]) * inv, tb = (hi[a] - oo[a]) * inv;
+        if (ta > tb) { const float x = ta; ta = tb; tb = x; }
+        t0 = fmaxf(t0, ta);
+        t1 = fminf(t1, tb);
+    }
+    return t0 <= t1 ? t0 * (1.0f - 0x1p-8f) : 0.0f;
+}
+
 // Starts path `local` in state slot `pid`: returns false for a slot outside the image;
-// otherwise initialises the state and returns the FP32 camera ray in (o, d).
+// otherwise initialises the state and returns the FP32 camera ray in (o, d). The FP32 ray
+// starts where the exact (double-float) camera ray enters the scene's bounding box (nodes:
+// the binary LBVH; no shift when n_tris is 0): the error bound of an FP32 triangle test
+// grows with the distance from the ray's origin (robust.cuh), and camera rays otherwise
+// cross the empty space between the camera and the scene first. The shift te is kept in
+// lpath.w and added back to the first hit's t (the depth AOV); the stored double-float ray
+// keeps the camera origin.
 __device__ __forceinline__ bool begin_path(const FrameParams& f, const PathDev& p, uint32_t pid, uint32_t local,
-                                           float3& o, float3& d) {
+                                           const float4* __restrict__ nodes, uint32_t n_tris, float3& o, float3& d) {
     const uint32_t j = local / f.slots;
     uint32_t x, y;
     slot_to_xy(local - j * f.slots, f.tiles_x, x, y);
@@ -146,10 +171,11 @@ __device__ __forceinline__ bool begin_path(const FrameParams& f, const PathDev& 
     ff3 ro, rd;
     camera_ray_ff(f, x, y, f.sample_base + j, ro, rd);
     ff_ray_store(&p.ray_ff[3ull * pid], ro, rd);
-    o = f.cam.origin;
     d = ff3_f(rd);
+    const float te = n_tris ? scene_entry(nodes, f.cam.origin, d) : 0.0f;
+    o = te > 0.0f ? ff3_f(ff3_add(ro, ff3_scale(rd, te))) : f.cam.origin;  // as ExactShifted
     p.beta[pid] = make_float4(1.f, 1.f, 1.f, 0.f);
-    p.lpath[pid] = make_float4(0.f, 0.f, 0.f, 0.f);
+    p.lpath[pid] = make_float4(0.f, 0.f, 0.f, te);
     p.aov_a[pid] = make_float4(0.f, 0.f, 0.f, 0.f);
     p.aov_n[pid] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (p.sig) p.sig[pid] = 0u;
@@ -160,13 +186,29 @@ __device__ __forceinline__ bool begin_path(const FrameParams& f, const PathDev& 
 // triangle); the result is hits[i] = (t, triangle or -1, 0, 0). The exact ray of path pid is
 // ray_ff[3 pid] (the path's double-float segment). A deferred ray leaves its certain result
 // in hits[i] for the fixup kernel.
+// The exact geometry of a closest-hit ray: the path's double-float ray, started te along
+// its direction (te: the shift of a camera ray's FP32 start, begin_path; 0 for the other
+// rays), the same point the FP32 ray was rounded from, so exact and FP32 distances agree.
+struct ExactShifted {
+    const float4* ray;
+    float te;
+    __device__ __forceinline__ void get(ff3& o, ff3& d) const {
+        ff_ray_load(ray, o, d);
+        if (te > 0.0f) o = ff3_add(o, ff3_scale(d, te));
+    }
+};
+
 struct ClosestJob {
     const float4* __restrict__ q;
     float4* __restrict__ hits;
     const float4* __restrict__ ray_ff;
+    const float4* __restrict__ lpath;  // .w: the camera ray's FP32 start shift (begin_path)
     DeferList deferred;
     __device__ __forceinline__ int pid(int i) const { return __float_as_int(q[2 * i].w); }
-    __device__ __forceinline__ ExactPtr exact(int i) const { return ExactPtr{ray_ff + 3ull * pid(i)}; }
+    __device__ __forceinline__ ExactShifted exact(int i) const {
+        const int id = pid(i);
+        return ExactShifted{ray_ff + 3ull * id, lpath[id].w};
+    }
     __device__ __forceinline__ void defer(int i, const TraceResult& r) const {
         store(i, r);
         deferred.push(i, r.undec);
@@ -288,8 +330,9 @@ __device__ __forceinline__ void shade_hit(const FrameParams& f, const SceneDev& 
     uint32_t sig = p.sig ? sig_mix(p.sig[pid], static_cast<uint32_t>(prim)) : 0u;
     if (bounce == 1) {
         const float3 em = xyz(__ldg(&s.emission[prim]));
+        const float te = p.lpath[pid].w;  // the camera ray's FP32 start shift (begin_path)
         p.lpath[pid] = make_float4(em.x, em.y, em.z, 0.f);
-        first_hit_aovs(alb, em, h.x, v.nrm, p.aov_a[pid], p.aov_n[pid]);
+        first_hit_aovs(alb, em, h.x + te, v.nrm, p.aov_a[pid], p.aov_n[pid]);
     }
     o.shadow = v.nee;
     if (v.nee) {

@@ -431,7 +431,7 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
         f.wave_offset = w * S;
         int* cnt = counters_.as<int>() + w * per_wave;
         R_TRY(QUASI_LAUNCH(prof_, "camera", s,
-                           (k_camera<<<ceil_div(Sw * slots, 256), 256, 0, s>>>(f, pd, queue_[0].as<float4>(), cnt))),
+                           (k_camera<<<ceil_div(Sw * slots, 256), 256, 0, s>>>(f, sd, pd, queue_[0].as<float4>(), cnt))),
               "camera");
         for (uint32_t k = 1; k <= D; ++k) {
             float4* qcur = queue_[(k - 1) & 1].as<float4>();
@@ -441,7 +441,7 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
             int* c_shadow = cnt + D + (k - 1);
             int* f_cur = cnt + 2 * D + (k - 1);
             int* f_shadow = cnt + 3 * D + (k - 1);
-            const ClosestJob cjob{qcur, hits_.as<float4>(), ray_ff_.as<float4>(),
+            const ClosestJob cjob{qcur, hits_.as<float4>(), ray_ff_.as<float4>(), lpath_.as<float4>(),
                                   DeferList{defer_.as<int2>(), cnt + 4 * D + (k - 1)}};
             const ShadowJob sjob{shadow_.as<float4>(), pd, DeferList{defer_.as<int2>(), cnt + 5 * D + (k - 1)}};
             R_TRY(QUASI_LAUNCH(prof_, "trace_closest", s,

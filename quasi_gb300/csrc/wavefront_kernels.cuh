@@ -42,11 +42,12 @@ __global__ void __launch_bounds__(256) k_pack_tris(const float* __restrict__ raw
     out[3 * i + 2] = make_float4(v[6], v[7], v[8], 0.f);
 }
 
-__global__ void __launch_bounds__(256) k_camera(FrameParams f, PathDev p, float4* __restrict__ q, int* __restrict__ q_count) {
+__global__ void __launch_bounds__(256) k_camera(FrameParams f, SceneDev s, PathDev p, float4* __restrict__ q,
+                                                int* __restrict__ q_count) {
     const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= f.wave_spp * f.slots) return;  // slots is a multiple of 32: whole warps leave
     float3 o = mk3(0.f, 0.f, 0.f), d = o;
-    const bool valid = begin_path(f, p, gid, gid, o, d);
+    const bool valid = begin_path(f, p, gid, gid, s.nodes, s.n_tris, o, d);
     const int pos = warp_append(0xffffffffu, valid, q_count);
     if (valid) {
         q[2 * pos] = make_float4(o.x, o.y, o.z, __int_as_float(static_cast<int>(gid)));
