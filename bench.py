@@ -30,6 +30,7 @@ METRIC = "Mrays/s at 1080p 64spp 1M tris; batched & backward Mrays/s at rel errâ
 SCENE = "soup:n=1000000,seed=0"
 WIDTH, HEIGHT, SPP, DEPTH = 1920, 1080, 64, 8
 WORKLOAD = "soup-1M 1920x1080 64spp depth8 NEE, LBVH rebuilt every frame"
+# a shadow ray reads 48 of its 64 queue bytes (the origin lo parts only when re-decided)
 TRI_BYTES, RAY_BYTES, HIT_BYTES, SHADOW_BYTES = 48, 32, 16, 48
 NODE_BYTES = {2: 64, 8: 96}  # binary LBVH node / 8-wide record
 

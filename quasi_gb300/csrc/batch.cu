@@ -163,8 +163,8 @@ int BatchRenderer::create(const Q_cuda_batch_scene* scenes, uint32_t count, cons
     for (uint32_t i = 0; i < count; ++i) {
         bvh_.emplace_back(new LbvhBuilder());
         const HostScene& h = scenes_[i];
-        B_TRY(bvh_[i]->build(tri_in_.as<float4>() + 3ull * h.tri_offset, h.n_tris, s, build_prof,
-                             err_dev_.as<uint32_t>()),
+        B_TRY(bvh_[i]->build(tri_in_.as<float4>() + 3ull * h.tri_offset, h.n_tris, emitters_.as<int>() + h.emit_offset,
+                             h.n_emit, s, build_prof, err_dev_.as<uint32_t>()),
               "lbvh build");
     }
     int rc = upload_table();
@@ -197,7 +197,6 @@ int BatchRenderer::upload_table() {
         d.s = SceneDev{tri_in_.as<float4>() + 3ull * h.tri_offset,
                        albedo_.as<float4>() + h.tri_offset,
                        emission_.as<float4>() + h.tri_offset,
-                       emitters_.as<int>() + h.emit_offset,
                        bv.nodes,
                        bv.tris,
                        h.n_tris,
@@ -207,7 +206,8 @@ int BatchRenderer::upload_table() {
                        nullptr,
                        0,
                        opt_.bvh_width == 2 ? nullptr : bv.wide,
-                       bv.tri_nrm};
+                       bv.tri_plane,
+                       bv.emit_tab};
         d.px_offset = h.px_offset;
         d.tri_offset = h.tri_offset;
         d.spp = h.spp;
@@ -369,7 +369,7 @@ int BatchRenderer::record_frame(cudaStream_t s, uint32_t& launches) {
                 int* f_cur = cnt + 2 * D + (k - 1);
                 int* f_shadow = cnt + 3 * D + (k - 1);
                 const ClosestJob cjob{qcur, hits_.as<float4>(), ray_ff_.as<float4>(), lpath_.as<float4>(),
-                                      DeferList{defer_.as<int2>(), cnt + 4 * D + (k - 1)}};
+                                      DeferList{defer_.as<int2>(), cnt + 4 * D + (k - 1)}, nullptr};
                 const ShadowJob sjob{shadow_.as<float4>(), pd, DeferList{defer_.as<int2>(), cnt + 5 * D + (k - 1)}};
                 B_TRY(QUASI_LAUNCH(prof_, "batch_trace_closest", s,
                                    (kc<<<grid_c, tb, smem_c_, s>>>(table, meta, cjob, c_cur, cap, chunk, refill, f_cur, err,
@@ -380,7 +380,7 @@ int BatchRenderer::record_frame(cudaStream_t s, uint32_t& launches) {
                                                                                         cnt + 6 * D + (k - 1), err))),
                       "batch_fixup_closest");
                 B_TRY(QUASI_LAUNCH(prof_, "batch_shade", s,
-                                   (k_batch_shade<<<grid_shade, 256, 0, s>>>(table, meta, pd, k, qcur, hits_.as<float4>(),
+                                   (k_batch_shade<<<grid_shade, 256, 0, s>>>(table, meta, pd, k, hits_.as<float4>(),
                                                                              c_cur, cap, qnext, k < D ? c_next : nullptr,
                                                                              shadow_.as<float4>(), c_shadow))),
                       "batch_shade");

@@ -177,6 +177,8 @@ __global__ void __launch_bounds__(256, WIDE ? QUASI_WIDE_MIN_BLOCKS : 1) k_batch
                                                              int capacity, int chunk, int refill, int* __restrict__ fetch,
                                                              uint32_t* __restrict__ err,
                                                              unsigned long long* __restrict__ stats) {
+    __shared__ int s_pid[256];
+    job.slot_pid = s_pid;
     const int n = min(*count, capacity);
     uint32_t e = 0;
     TraceCounters c;
@@ -252,9 +254,9 @@ __global__ void __launch_bounds__(128) k_batch_fixup(const BatchSceneDev* __rest
     if (e) atomicOr(err, e);
 }
 
-__global__ void __launch_bounds__(256) k_batch_shade(const BatchSceneDev* __restrict__ scenes,
+__global__ void __launch_bounds__(256, QUASI_SHADE_MIN_BLOCKS) k_batch_shade(const BatchSceneDev* __restrict__ scenes,
                                                      const uint2* __restrict__ meta, PathDev p, uint32_t bounce,
-                                                     const float4* __restrict__ q, const float4* __restrict__ hits,
+                                                     const float4* __restrict__ hits,
                                                      const int* __restrict__ count, int capacity,
                                                      float4* __restrict__ next_q, int* __restrict__ next_count,
                                                      float4* __restrict__ shadow_q, int* __restrict__ shadow_count) {
@@ -263,22 +265,21 @@ __global__ void __launch_bounds__(256) k_batch_shade(const BatchSceneDev* __rest
     const int stride = gridDim.x * blockDim.x;
     for (int base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; base < n; base += stride) {
         const int i = base + lane;
-        HitShade o;
-        o.shadow = o.next = false;
-        int pid = 0, prim = -1;
+        int pid = 0;
+        uint2 m = make_uint2(0u, 0u);  // scene 0 stands in for lanes without a hit (not read)
+        float4 h = make_float4(0.f, __int_as_float(-1), 0.f, 0.f);
         if (i < n) {
-            const float4 h = hits[i];
-            pid = __float_as_int(q[2 * i].w);
-            prim = __float_as_int(h.y);
-            if (prim < 0) {
+            h = hits[i];
+            pid = __float_as_int(h.z);
+            if (__float_as_int(h.y) < 0) {
                 if (p.sig) p.sig[pid] = sig_mix(p.sig[pid], k_sig_miss);
             } else {
-                const uint2 m = meta[pid];
-                const BatchSceneDev& b = scenes[m.x];
-                shade_hit(b.f, b.s, p, bounce, pid, m.y, h, o);
+                m = meta[pid];
             }
         }
-        enqueue_shaded(i < n && prim >= 0, pid, prim, o, shadow_q, shadow_count, next_q, next_count);
+        const BatchSceneDev& b = scenes[m.x];
+        shade_and_enqueue(i < n && __float_as_int(h.y) >= 0, b.f, b.s, p, bounce, pid, m.y, h, shadow_q,
+                          shadow_count, next_q, next_count);
     }
 }
 

@@ -486,20 +486,47 @@ __global__ void __launch_bounds__(128) k_collapse8(const float4* __restrict__ no
     w[5] = make_float4(__int_as_float(refs[4]), __int_as_float(refs[5]), __int_as_float(refs[6]), __int_as_float(refs[7]));
 }
 
-// Shading geometry of triangle i (original order): ng = cross(e1, e2) in double-float from
-// the exact edge differences, its length |ng| and the unit normal ng / |ng| (one reciprocal).
-__global__ void __launch_bounds__(256) k_tri_normals(const float4* __restrict__ tri_in, uint32_t n,
-                                                     float4* __restrict__ out) {
+// Unit normal u = ng / |ng| of the triangle (a, b, c), ng = cross(e1, e2) in double-float from
+// the exact edge differences (one reciprocal); len = |ng| (twice the area). Shared by the
+// plane and emitter tables so both hold the same bits.
+__device__ __forceinline__ ff3 tri_unit_normal_ff(float3 a, float3 b, float3 c, ff& len) {
+    const ff3 e1 = ff3_diff(b, a), e2 = ff3_diff(c, a);
+    const ff3 ng = ff3_cross(e1, e2);
+    len = ff3_length(ng);
+    return ff3_scale(ng, ff_div(ffv(1.0f), len));
+}
+
+// Shading plane of triangle i (original order): the unit normal u and the plane offset u.v0,
+// double-float; 32 bytes, one sector per hit.
+__global__ void __launch_bounds__(256) k_tri_planes(const float4* __restrict__ tri_in, uint32_t n,
+                                                    float4* __restrict__ out) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float3 a = xyz(__ldg(&tri_in[3 * i]));
-    const ff3 e1 = ff3_diff(xyz(__ldg(&tri_in[3 * i + 1])), a);
-    const ff3 e2 = ff3_diff(xyz(__ldg(&tri_in[3 * i + 2])), a);
-    const ff3 ng = ff3_cross(e1, e2);
-    const ff len = ff3_length(ng);
-    const ff3 u = ff3_scale(ng, ff_div(ffv(1.0f), len));
+    ff len;
+    const ff3 u = tri_unit_normal_ff(a, xyz(__ldg(&tri_in[3 * i + 1])), xyz(__ldg(&tri_in[3 * i + 2])), len);
+    const ff off = ff3_dot(u, ff3v(a));
     out[2 * i] = make_float4(u.x.hi, u.x.lo, u.y.hi, u.y.lo);
-    out[2 * i + 1] = make_float4(u.z.hi, u.z.lo, len.hi, len.lo);
+    out[2 * i + 1] = make_float4(u.z.hi, u.z.lo, off.hi, off.lo);
+}
+
+// Light-sampling record of emitter slot k (triangle l = emitters[k]), 5 float4:
+// (v0, l), (v1, |ng|.hi), (v2, |ng|.lo), (u.x, u.y), (u.z, -, -) with u and |ng| as in
+// k_tri_planes. One record per light sample replaces the emitter index and the light
+// triangle's vertex and table loads that depend on it.
+__global__ void __launch_bounds__(256) k_emit_table(const float4* __restrict__ tri_in, const int* __restrict__ emitters,
+                                                    uint32_t n_emit, float4* __restrict__ out) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_emit) return;
+    const int l = __ldg(&emitters[k]);
+    const float3 a = xyz(__ldg(&tri_in[3 * l])), b = xyz(__ldg(&tri_in[3 * l + 1])), c = xyz(__ldg(&tri_in[3 * l + 2]));
+    ff len;
+    const ff3 u = tri_unit_normal_ff(a, b, c, len);
+    out[5 * k] = make_float4(a.x, a.y, a.z, __int_as_float(l));
+    out[5 * k + 1] = make_float4(b.x, b.y, b.z, len.hi);
+    out[5 * k + 2] = make_float4(c.x, c.y, c.z, len.lo);
+    out[5 * k + 3] = make_float4(u.x.hi, u.x.lo, u.y.hi, u.y.lo);
+    out[5 * k + 4] = make_float4(u.z.hi, u.z.lo, 0.f, 0.f);
 }
 
 // Copies the first `count` internal nodes in breadth-first order (the top levels of the
@@ -615,7 +642,7 @@ cudaError_t LbvhBuilder::reserve(uint32_t n) {
     QUASI_TRY_CUDA(cudaMalloc(&nodes_, sizeof(float4) * 4 * m));
     QUASI_TRY_CUDA(cudaMalloc(&tris_, sizeof(float4) * 3 * m));
     QUASI_TRY_CUDA(cudaMalloc(&wide_, sizeof(float4) * k_wide_node_f4 * m));
-    QUASI_TRY_CUDA(cudaMalloc(&tri_nrm_, sizeof(float4) * 2 * m));
+    QUASI_TRY_CUDA(cudaMalloc(&tri_plane_, sizeof(float4) * 2 * m));
     QUASI_TRY_CUDA(radix_sort_reserve(sort_, m));
     capacity_ = m;
     return cudaSuccess;
@@ -625,12 +652,13 @@ void LbvhBuilder::release() {
     for (void* p : {static_cast<void*>(bounds_), static_cast<void*>(partial_), static_cast<void*>(morton_),
                     static_cast<void*>(keys_), static_cast<void*>(order_), static_cast<void*>(parent_),
                     static_cast<void*>(flags_), static_cast<void*>(nodes_), static_cast<void*>(tris_),
-                    static_cast<void*>(wide_), static_cast<void*>(tri_nrm_)})
+                    static_cast<void*>(wide_), static_cast<void*>(tri_plane_), static_cast<void*>(emit_tab_)})
         if (p) cudaFree(p);
     bounds_ = partial_ = nullptr;
     morton_ = keys_ = order_ = flags_ = nullptr;
     parent_ = nullptr;
-    nodes_ = tris_ = wide_ = tri_nrm_ = nullptr;
+    nodes_ = tris_ = wide_ = tri_plane_ = emit_tab_ = nullptr;
+    emit_capacity_ = 0;
     if (tree_) cudaFree(tree_);
     tree_ = nullptr;
     tree_n_ = tree_capacity_ = 0;
@@ -639,13 +667,25 @@ void LbvhBuilder::release() {
     n_ = 0;
 }
 
-cudaError_t LbvhBuilder::build(const float4* tri_in, uint32_t n, cudaStream_t stream, KernelProfiler& prof,
-                               uint32_t* err) {
+cudaError_t LbvhBuilder::build(const float4* tri_in, uint32_t n, const int* emitters, uint32_t n_emit,
+                               cudaStream_t stream, KernelProfiler& prof, uint32_t* err) {
     QUASI_TRY_CUDA(reserve(n));
     n_ = n;
     if (n == 0) return cudaSuccess;
-    QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "tri_normals", stream,
-                                (k_tri_normals<<<ceil_div(n, 256), 256, 0, stream>>>(tri_in, n, tri_nrm_))));
+    QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "tri_planes", stream,
+                                (k_tri_planes<<<ceil_div(n, 256), 256, 0, stream>>>(tri_in, n, tri_plane_))));
+    if (n_emit > 0) {
+        if (n_emit > emit_capacity_) {
+            if (emit_tab_) cudaFree(emit_tab_);
+            emit_tab_ = nullptr;
+            emit_capacity_ = 0;
+            QUASI_TRY_CUDA(cudaMalloc(&emit_tab_, sizeof(float4) * 5 * n_emit));
+            emit_capacity_ = n_emit;
+        }
+        QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "emit_table", stream,
+                                    (k_emit_table<<<ceil_div(n_emit, 256), 256, 0, stream>>>(tri_in, emitters, n_emit,
+                                                                                             emit_tab_))));
+    }
     const int parts = static_cast<int>(std::min<uint32_t>(k_bounds_blocks, ceil_div(n, 256)));
     QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_bounds", stream,
                                 (k_bounds_partial<<<parts, 256, 0, stream>>>(tri_in, n, partial_))));

@@ -52,8 +52,9 @@ struct LbvhView {
     const float4* tree = nullptr;   // top levels in breadth-first order (for shared memory)
     int tree_n = 0;                 // nodes in `tree`
     const float4* wide = nullptr;   // 8-wide records (wide.cuh), one per internal node
-    const float4* tri_nrm = nullptr; // per triangle (original order), 2 float4: the unit normal
-                                     // of cross(e1, e2) and that vector's length, double-float
+    const float4* tri_plane = nullptr; // per triangle (original order), 2 float4: the unit normal
+                                       // of cross(e1, e2) and the plane offset n.v0, double-float
+    const float4* emit_tab = nullptr;  // per emitter slot, 5 float4 (k_emit_table)
 };
 
 class LbvhBuilder {
@@ -67,14 +68,18 @@ public:
     void release();
 
     // tri_in: 3 float4 per triangle (v0, v1, v2; w ignored), original order, device.
+    // emitters: the n_emit emitting triangles (indices into tri_in), device; their
+    // light-sampling records are rebuilt with the hierarchy.
     // err: device word that receives QUASI_DEVERR_* bits if the hierarchy is malformed.
-    cudaError_t build(const float4* tri_in, uint32_t n, cudaStream_t stream, KernelProfiler& prof, uint32_t* err);
+    cudaError_t build(const float4* tri_in, uint32_t n, const int* emitters, uint32_t n_emit, cudaStream_t stream,
+                      KernelProfiler& prof, uint32_t* err);
 
     // Copies the top max_nodes internal nodes (breadth first) for staging in shared memory.
     cudaError_t build_treelet(int max_nodes, cudaStream_t stream, KernelProfiler& prof);
 
     LbvhView view() const {
-        return LbvhView{nodes_, tris_, n_, n_ == 0 ? 0u : (n_ > 1 ? n_ - 1 : 1u), tree_, tree_n_, wide_, tri_nrm_};
+        return LbvhView{nodes_, tris_, n_, n_ == 0 ? 0u : (n_ > 1 ? n_ - 1 : 1u), tree_, tree_n_, wide_, tri_plane_,
+                        emit_tab_};
     }
 
     // Debug copies to host (stream-synchronous).
@@ -96,7 +101,9 @@ private:
     float4* nodes_ = nullptr;
     float4* tris_ = nullptr;
     float4* wide_ = nullptr;         // 8-wide records, 96 bytes per internal node
-    float4* tri_nrm_ = nullptr;      // 32 bytes per triangle (shading normals and areas)
+    float4* tri_plane_ = nullptr;    // 32 bytes per triangle (shading normal and plane offset)
+    float4* emit_tab_ = nullptr;     // 80 bytes per emitter (light-sampling records)
+    uint32_t emit_capacity_ = 0;
     float4* tree_ = nullptr;
     int tree_n_ = 0;
     int tree_capacity_ = 0;

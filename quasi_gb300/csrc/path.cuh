@@ -37,7 +37,6 @@ struct SceneDev {
     const float4* tri_in;   // original order, v0 v1 v2
     const float4* albedo;
     const float4* emission;
-    const int* emitters;
     const float4* nodes;
     const float4* tris;     // leaf order, v0+orig, e1, e2
     uint32_t n_tris, n_emit;
@@ -47,7 +46,8 @@ struct SceneDev {
     int tree_n;             // nodes in `tree` (0 = no staging)
     const float4* wide;     // 8-wide traversal records (wide.cuh) for the wavefront trace
                             // kernels, or null: they traverse `nodes`
-    const float4* tri_nrm;  // per triangle: unit normal and |cross(e1, e2)|, double-float
+    const float4* tri_plane;  // per triangle: unit normal and plane offset n.v0, double-float
+    const float4* emit_tab;   // per emitter slot: light-sampling record, 5 float4 (k_emit_table)
 };
 
 // Copies the treelet into the block's shared memory (dynamic size tree_n * 64 bytes).
@@ -183,9 +183,9 @@ __device__ __forceinline__ bool begin_path(const FrameParams& f, const PathDev& 
 }
 
 // Closest-hit queue: ray i is q[2i] = (origin, path id), q[2i+1] = (direction, excluded
-// triangle); the result is hits[i] = (t, triangle or -1, 0, 0). The exact ray of path pid is
-// ray_ff[3 pid] (the path's double-float segment). A deferred ray leaves its certain result
-// in hits[i] for the fixup kernel.
+// triangle); the result is hits[i] = (t, triangle or -1, path id, 0), so shading reads the
+// path id with the hit. The exact ray of path pid is ray_ff[3 pid] (the path's double-float
+// segment). A deferred ray leaves its certain result in hits[i] for the fixup kernel.
 // The exact geometry of a closest-hit ray: the path's double-float ray, started te along
 // its direction (te: the shift of a camera ray's FP32 start, begin_path; 0 for the other
 // rays), the same point the FP32 ray was rounded from, so exact and FP32 distances agree.
@@ -204,6 +204,9 @@ struct ClosestJob {
     const float4* __restrict__ ray_ff;
     const float4* __restrict__ lpath;  // .w: the camera ray's FP32 start shift (begin_path)
     DeferList deferred;
+    // Set by the trace kernels: one shared-memory word per thread that carries the path id of
+    // the thread's ray from load() to store(); null: store() reads it from the queue.
+    int* slot_pid;
     __device__ __forceinline__ int pid(int i) const { return __float_as_int(q[2 * i].w); }
     __device__ __forceinline__ ExactShifted exact(int i) const {
         const int id = pid(i);
@@ -227,9 +230,11 @@ struct ClosestJob {
         d = xyz(r1);
         tmax = __int_as_float(0x7f800000);
         exclude = __float_as_int(r1.w);
+        if (slot_pid) slot_pid[threadIdx.x] = __float_as_int(r0.w);
     }
     __device__ __forceinline__ void store(int i, const TraceResult& s) const {
-        hits[i] = make_float4(s.t, __int_as_float(s.prim), 0.f, 0.f);
+        const int id = slot_pid ? slot_pid[threadIdx.x] : pid(i);
+        hits[i] = make_float4(s.t, __int_as_float(s.prim), __int_as_float(id), 0.f);
     }
 };
 
@@ -297,83 +302,89 @@ constexpr int k_mode_refill = 2;      // per-lane refill (trace_persistent)
 constexpr int k_mode_wide = 3;        // warp batches over the 8-wide records (trace_batches_wide)
 constexpr int k_mode_wide_refill = 4; // per-lane refill over the 8-wide records (trace_wide_refill)
 
-// What shading one closest hit asks the wavefront to enqueue.
-struct HitShade {
-    bool shadow;            // enqueue the shadow ray (so, sd, stmax) carrying `contrib`
-    bool next;              // enqueue the continuation ray (norg, nd)
-    float3 contrib;
-    float3 so, sd;
-    float3 so_lo;           // lo parts of the exact (double-float) shadow ray origin
-    float stmax;
-    float3 norg, nd;
-};
+// Minimum resident 256-thread blocks per SM asked of the compiler for k_shade and
+// k_batch_shade (a register cap). Before the shading table k_shade took 141 registers
+// uncapped and the 1080p frame's shading cost 138 ms; 2 blocks (128 registers) or 4 (64,
+// with spills) cost 101 ms on GB300. With the continuation finished before the light sample
+// (shade_and_enqueue) it fits 80 registers without spills at 3 blocks.
+#ifndef QUASI_SHADE_MIN_BLOCKS
+#define QUASI_SHADE_MIN_BLOCKS 3
+#endif
 
-// Shades the closest hit h = (t, prim >= 0, u, v) at bounce `bounce` of path `local` (state
-// slot `pid`): first-hit emission and AOVs, the NEE sample and the continuation direction.
-// Updates beta, the signature and the stored double-float ray of the path.
-__device__ __forceinline__ void shade_hit(const FrameParams& f, const SceneDev& s, const PathDev& p, uint32_t bounce,
-                                          int pid, uint32_t local, float4 h, HitShade& o) {
-    const VertexScene vs{s.tri_in, s.tri_nrm, s.albedo, s.emission, s.emitters, s.n_emit, f.eps};
+// Shades the closest hit h = (t, prim, u, v) at bounce `bounce` of path `local` (state slot
+// `pid`) and enqueues the rays it asks for; all lanes of the warp call it, `active` lanes
+// hold a hit (prim >= 0), and f and s are only read for them. In order: the hit point,
+// first-hit emission and AOVs, beta; the continuation ray (stored double-float ray and next
+// queue); then the NEE sample (shadow queue) and the signature. Finishing the continuation
+// before the light triangle is loaded keeps fewer values live at once than computing both
+// from one set of loads; the values are those of shade_vertex.
+__device__ __forceinline__ void shade_and_enqueue(bool active, const FrameParams& f, const SceneDev& s,
+                                                  const PathDev& p, uint32_t bounce, int pid, uint32_t local,
+                                                  float4 h, float4* __restrict__ shadow_q,
+                                                  int* __restrict__ shadow_count, float4* __restrict__ next_q,
+                                                  int* __restrict__ next_count) {
     const int prim = __float_as_int(h.y);
-    ff3 ro, rd;
-    ff_ray_load(&p.ray_ff[3ull * pid], ro, rd);
-    const uint32_t j = local / f.slots;
-    uint32_t px, py;
-    slot_to_xy(local - j * f.slots, f.tiles_x, px, py);
-    const uint32_t key = path_key(f.seed, py * f.width + px, f.sample_base + j, bounce);
-    const float3 alb = xyz(__ldg(&s.albedo[prim]));
-    const float3 beta = xyz(p.beta[pid]);
-    const float3 nb = beta * alb;
-    const bool cont = bounce < f.max_depth && max3(nb) > 0.0f;
-    VertexResult v;
-    shade_vertex(vs, key, prim, h, ro, rd, cont, v);
-    uint32_t sig = p.sig ? sig_mix(p.sig[pid], static_cast<uint32_t>(prim)) : 0u;
-    if (bounce == 1) {
-        const float3 em = xyz(__ldg(&s.emission[prim]));
-        const float te = p.lpath[pid].w;  // the camera ray's FP32 start shift (begin_path)
-        p.lpath[pid] = make_float4(em.x, em.y, em.z, 0.f);
-        first_hit_aovs(alb, em, h.x + te, v.nrm, p.aov_a[pid], p.aov_n[pid]);
+    ff3 x{}, nrm{}, org{};
+    float3 nb = mk3(0.f, 0.f, 0.f);
+    bool cont = false;
+    VertexRandom r{};
+    if (active) {
+        const VertexScene vs{s.tri_plane, s.emit_tab, s.n_emit, f.eps};
+        ff3 ro, rd;
+        ff_ray_load(&p.ray_ff[3ull * pid], ro, rd);
+        const uint32_t j = local / f.slots;
+        uint32_t px, py;
+        slot_to_xy(local - j * f.slots, f.tiles_x, px, py);
+        r = vertex_random(path_key(f.seed, py * f.width + px, f.sample_base + j, bounce));
+        const float3 alb = xyz(__ldg(&s.albedo[prim]));
+        nb = xyz(p.beta[pid]) * alb;
+        cont = bounce < f.max_depth && max3(nb) > 0.0f;
+        vertex_point(vs, prim, ro, rd, x, nrm);
+        org = vertex_origin(vs, x, nrm);
+        if (bounce == 1) {
+            const float3 em = xyz(__ldg(&s.emission[prim]));
+            const float te = p.lpath[pid].w;  // the camera ray's FP32 start shift (begin_path)
+            p.lpath[pid] = make_float4(em.x, em.y, em.z, 0.f);
+            first_hit_aovs(alb, em, h.x + te, ff3_f(nrm), p.aov_a[pid], p.aov_n[pid]);
+        }
+        p.beta[pid] = make_float4(nb.x, nb.y, nb.z, 0.f);
     }
-    o.shadow = v.nee;
-    if (v.nee) {
-        o.contrib = beta * alb * xyz(__ldg(&s.emission[v.light])) * v.g;
-        o.so = v.so;
-        o.so_lo = mk3(v.seg_o.x.lo, v.seg_o.y.lo, v.seg_o.z.lo);
-        o.sd = v.sd;
-        o.stmax = v.stmax;
-    } else {
-        sig = sig_mix(sig, k_sig_no_nee);
+    // The continuation ray.
+    float3 nd = mk3(0.f, 0.f, 0.f);
+    if (active && cont) {
+        const ff3 dir = vertex_dir(nrm, r.r3, r.r4);
+        ff_ray_store(&p.ray_ff[3ull * pid], org, dir);
+        nd = ff3_f(dir);
     }
-    p.beta[pid] = make_float4(nb.x, nb.y, nb.z, 0.f);
-    if (p.sig) p.sig[pid] = sig;
-    o.next = cont;
-    if (cont) {
-        ff_ray_store(&p.ray_ff[3ull * pid], v.org, v.dir);
-        o.norg = ff3_f(v.org);
-        o.nd = ff3_f(v.dir);
-    } else if (v.nee) {
-        // the shadow segment's end, for its exact re-decision (ExactSeg)
-        ff_ray_store(&p.ray_ff[3ull * pid], v.org, ff3{});
-    }
-}
-
-// Enqueues the rays one shading step produced (all lanes of the warp call it).
-__device__ __forceinline__ void enqueue_shaded(bool active, int pid, int prim, const HitShade& o,
-                                               float4* __restrict__ shadow_q, int* __restrict__ shadow_count,
-                                               float4* __restrict__ next_q, int* __restrict__ next_count) {
-    const bool want_shadow = active && o.shadow;
-    const bool want_next = active && o.next && next_count != nullptr;
-    const int ps = warp_append(0xffffffffu, want_shadow, shadow_count);
-    if (want_shadow) {
-        shadow_q[4 * ps] = make_float4(o.so.x, o.so.y, o.so.z, __int_as_float(pid));
-        shadow_q[4 * ps + 1] = make_float4(o.sd.x, o.sd.y, o.sd.z, o.stmax);
-        shadow_q[4 * ps + 2] = make_float4(o.contrib.x, o.contrib.y, o.contrib.z, o.so_lo.x);
-        shadow_q[4 * ps + 3] = make_float4(o.so_lo.y, o.so_lo.z, 0.f, 0.f);
-    }
+    const bool want_next = active && cont && next_count != nullptr;
     const int pn = warp_append(0xffffffffu, want_next, next_count);
     if (want_next) {
-        next_q[2 * pn] = make_float4(o.norg.x, o.norg.y, o.norg.z, __int_as_float(pid));
-        next_q[2 * pn + 1] = make_float4(o.nd.x, o.nd.y, o.nd.z, __int_as_float(prim));
+        const float3 no = ff3_f(org);
+        next_q[2 * pn] = make_float4(no.x, no.y, no.z, __int_as_float(pid));
+        next_q[2 * pn + 1] = make_float4(nd.x, nd.y, nd.z, __int_as_float(prim));
+    }
+    // The NEE sample.
+    VertexResult v;
+    v.nee = false;
+    if (active) {
+        const VertexScene vs{s.tri_plane, s.emit_tab, s.n_emit, f.eps};
+        const LightTri lt = load_light(vs, r.sel);
+        vertex_light(vs, prim, lt, r.r1, r.r2, x, nrm, org, v);
+        // without a continuation the stored ray keeps only the shadow segment's end (ExactSeg)
+        if (v.nee && !cont) ff_ray_store(&p.ray_ff[3ull * pid], org, ff3{});
+    }
+    const int ps = warp_append(0xffffffffu, v.nee, shadow_count);
+    if (v.nee) {
+        const float3 contrib = nb * xyz(__ldg(&s.emission[v.light])) * v.g;
+        shadow_q[4 * ps] = make_float4(v.so.x, v.so.y, v.so.z, __int_as_float(pid));
+        shadow_q[4 * ps + 1] = make_float4(v.sd.x, v.sd.y, v.sd.z, v.stmax);
+        shadow_q[4 * ps + 2] = make_float4(contrib.x, contrib.y, contrib.z, v.seg_o.x.lo);
+        shadow_q[4 * ps + 3] = make_float4(v.seg_o.y.lo, v.seg_o.z.lo, 0.f, 0.f);
+    }
+    if (active && p.sig) {
+        uint32_t sig = sig_mix(p.sig[pid], static_cast<uint32_t>(prim));
+        if (!v.nee) sig = sig_mix(sig, k_sig_no_nee);
+        p.sig[pid] = sig;
     }
 }
 
@@ -429,7 +440,7 @@ __device__ __forceinline__ float3 trace_path(const FrameParams& f, const SceneDe
                                              uint32_t sample, PathVertex* verts, int& n_verts, float4* aov_a,
                                              float4* aov_n, uint32_t* sig_out, uint32_t& err, TraceCounters& cnt,
                                              int& rays, int& shadow_rays, float pad) {
-    const VertexScene vs{s.tri_in, s.tri_nrm, s.albedo, s.emission, s.emitters, s.n_emit, f.eps};
+    const VertexScene vs{s.tri_plane, s.emit_tab, s.n_emit, f.eps};
     ff3 ro, rd;
     camera_ray_ff(f, x, y, sample, ro, rd);
     float3 beta = mk3(1.f, 1.f, 1.f), L = mk3(0.f, 0.f, 0.f);

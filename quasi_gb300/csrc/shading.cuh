@@ -5,7 +5,8 @@
 // Per vertex k of a path (hit triangle h, incoming double-float ray ro + t rd):
 //   x   = plane(h) intersected with the double-float ray        (hit point)
 //   n   = normalize(cross(e1, e2)) flipped to face the ray       (plugin.mm:192); the unit
-//         normals and |cross(e1, e2)| come from a per-triangle table built with the LBVH
+//         normal and the plane offset n.v0 come from a per-triangle table built with the
+//         LBVH, the light triangle's data from a per-emitter record built with it
 //   key = path_key(seed, pixel, sample, k);  sel = pcg(key); r1, r2, r3, r4 chained
 //   NEE: light l = emitters[(sel * n_emit) >> 32], point y = v0 + su(1-r2) e1 + su r2 e2,
 //        su = sqrt(r1); g = cos_x cos_l / d^2 * area * n_emit / pi, skipped when l == h or a
@@ -23,11 +24,8 @@
 namespace quasi {
 
 struct VertexScene {
-    const float4* tri_in;   // original order, v0 v1 v2
-    const float4* tri_nrm;  // original order: unit normal of cross(e1, e2), |cross(e1, e2)|
-    const float4* albedo;
-    const float4* emission;
-    const int* emitters;
+    const float4* tri_plane;  // original order: unit normal of cross(e1, e2) and the plane offset n.v0
+    const float4* emit_tab;   // per emitter slot: (v0, l), (v1, |ng|.hi), (v2, |ng|.lo), (n.x, n.y), (n.z)
     uint32_t n_emit;
     float eps;
 };
@@ -50,115 +48,150 @@ __device__ __forceinline__ float fdot3(float3 a, float3 b) {
     return __fmaf_rn(a.z, b.z, __fmaf_rn(a.y, b.y, __fmul_rn(a.x, b.x)));
 }
 
-// Unit normal and |cross(e1, e2)| (twice the area) of triangle i from the shading table.
-__device__ __forceinline__ ff3 tri_unit_normal(const float4* __restrict__ tri_nrm, int i, ff& area2) {
-    const float4 p = __ldg(&tri_nrm[2 * i]), q = __ldg(&tri_nrm[2 * i + 1]);
-    area2 = ff{q.z, q.w};
-    return ff3{ff{p.x, p.y}, ff{p.z, p.w}, ff{q.x, q.y}};
+// The random numbers of one vertex, from its path key: sel picks the light, (r1, r2) the
+// point on it, (r3, r4) the continuation direction.
+struct VertexRandom {
+    uint32_t sel;
+    float r1, r2, r3, r4;
+};
+
+__device__ __forceinline__ VertexRandom vertex_random(uint32_t key) {
+    VertexRandom r;
+    uint32_t st = key;
+    r.sel = pcg_hash(st);
+    st = r.sel;
+    r.r1 = rng_next(st);
+    r.r2 = rng_next(st);
+    r.r3 = rng_next(st);
+    r.r4 = rng_next(st);
+    return r;
 }
 
-// hit: (t, prim, -, -) from the traversal; ro, rd: the double-float ray that found it.
-__device__ __forceinline__ void shade_vertex(const VertexScene& s, uint32_t key, int prim, float4 hit, const ff3& ro,
-                                             const ff3& rd, bool want_dir, VertexResult& out) {
-    // The light choice depends only on the path key: start its dependent loads (emitter
-    // index, then the light triangle and its table entry) before the hit-point arithmetic so
-    // their latency overlaps it.
-    uint32_t st = key;
-    const uint32_t sel = pcg_hash(st);
-    st = sel;
-    const float r1 = rng_next(st);
-    const float r2 = rng_next(st);
-    int l = -1;
-    float4 lv0 = make_float4(0.f, 0.f, 0.f, 0.f), lv1 = lv0, lv2 = lv0, ln0 = lv0, ln1 = lv0;
+// The light-sampling record of the emitter a vertex's NEE sample picked (l = -1 without
+// emitters): the triangle's vertices, |cross(e1, e2)| and unit normal (k_emit_table).
+struct LightTri {
+    int l;
+    float4 v0, v1, v2, n0, n1;
+};
+
+__device__ __forceinline__ LightTri load_light(const VertexScene& s, uint32_t sel) {
+    LightTri t;
+    t.l = -1;
+    t.v0 = t.v1 = t.v2 = t.n0 = t.n1 = make_float4(0.f, 0.f, 0.f, 0.f);
     if (s.n_emit > 0) {
-        l = __ldg(&s.emitters[static_cast<uint32_t>((static_cast<uint64_t>(sel) * s.n_emit) >> 32)]);
-        if (l != prim) {
-            lv0 = __ldg(&s.tri_in[3 * l]);
-            lv1 = __ldg(&s.tri_in[3 * l + 1]);
-            lv2 = __ldg(&s.tri_in[3 * l + 2]);
-            ln0 = __ldg(&s.tri_nrm[2 * l]);
-            ln1 = __ldg(&s.tri_nrm[2 * l + 1]);
-        }
+        const float4* r = s.emit_tab + 5ull * static_cast<uint32_t>((static_cast<uint64_t>(sel) * s.n_emit) >> 32);
+        t.v0 = __ldg(&r[0]);
+        t.v1 = __ldg(&r[1]);
+        t.v2 = __ldg(&r[2]);
+        t.n0 = __ldg(&r[3]);
+        t.n1 = __ldg(&r[4]);
+        t.l = __float_as_int(t.v0.w);
     }
-    const float3 a = xyz(__ldg(&s.tri_in[3 * prim]));
-    ff area_h;
-    ff3 nrm = tri_unit_normal(s.tri_nrm, prim, area_h);
-    // Re-intersect the hit triangle's plane with the double-float ray.
+    return t;
+}
+
+// The hit point x (the hit triangle's plane n.x = n.v0 intersected with the double-float ray
+// ro + t rd, t = (n.v0 - n.ro) / n.rd) and the unit normal facing the ray.
+__device__ __forceinline__ void vertex_point(const VertexScene& s, int prim, const ff3& ro, const ff3& rd, ff3& x,
+                                             ff3& nrm) {
+    const float4 p = __ldg(&s.tri_plane[2 * prim]), q = __ldg(&s.tri_plane[2 * prim + 1]);
+    nrm = ff3{ff{p.x, p.y}, ff{p.z, p.w}, ff{q.x, q.y}};
     const ff den = ff3_dot(nrm, rd);
-    ff3 x;
     if (den.hi != 0.0f) {
-        const ff t = ff_div(ff3_dot(nrm, ff3_sub(ff3v(a), ro)), den);
+        const ff t = ff_div(ff_sub(ff{q.z, q.w}, ff3_dot(nrm, ro)), den);
         x = ff3_add(ro, ff3_scale(rd, t));
     } else {
         // A ray parallel to the plane cannot hit the triangle (an exact hit needs
         // det = -d.(e1 x e2) != 0); kept only so that x is defined.
-        x = ff3v(a);
+        x = ro;
     }
     if (den.hi > 0.0f) nrm = ff3_neg(nrm);
-    out.nrm = ff3_f(nrm);
-    out.org = ff3_add(x, ff3_scale(nrm, s.eps));
+}
+
+// Continuation origin x + eps n.
+__device__ __forceinline__ ff3 vertex_origin(const VertexScene& s, const ff3& x, const ff3& nrm) {
+    return ff3_add(x, ff3_scale(nrm, s.eps));
+}
+
+// Cosine-weighted continuation direction about nrm (plugin.mm:111-125) in double-float:
+// phi = 2 pi r3, cos = sqrt(1 - r4), sin = sqrt(r4).
+__device__ __forceinline__ ff3 vertex_dir(const ff3& nrm, float r3, float r4) {
+    ff sphi, cphi;
+    ff_sincospi(2.0f * r3, sphi, cphi);
+    const ff cos_t = ff_sqrt(two_sum(1.0f, -r4));
+    const ff sin_t = ff_sqrt(ffv(r4));
+    // v = normalize(cross(w, a)), a = (0,1,0) if |w.x| > 0.9 else (1,0,0)
+    ff3 vv = fabsf(nrm.x.hi) > 0.9f ? ff3{ff_neg(nrm.z), ffv(0.0f), nrm.x} : ff3{ffv(0.0f), nrm.z, ff_neg(nrm.y)};
+    vv = ff3_normalize(vv);
+    const ff3 uu = ff3_cross(nrm, vv);
+    // (uu, vv, nrm) is orthonormal to ~1e-14 and cos^2 + sin^2 = 1, so the direction is a
+    // unit vector to that accuracy without the final normalisation of plugin.mm:124.
+    return ff3_add(ff3_add(ff3_scale(uu, ff_mul(cphi, sin_t)), ff3_scale(vv, ff_mul(sphi, sin_t))),
+                   ff3_scale(nrm, cos_t));
+}
+
+// The NEE sample of a vertex at x (normal nrm, continuation origin org) towards the light
+// triangle lt: sets nee, light, g, the FP32 shadow ray and the exact segment.
+__device__ __forceinline__ void vertex_light(const VertexScene& s, int prim, const LightTri& lt, float r1, float r2,
+                                             const ff3& x, const ff3& nrm, const ff3& org, VertexResult& out) {
     out.nee = false;
     out.light = -1;
     out.g = 0.0f;
-    if (s.n_emit > 0) {
-        if (l != prim) {
-            const float3 la = xyz(lv0);
-            const ff3 le1 = ff3_diff(xyz(lv1), la);
-            const ff3 le2 = ff3_diff(xyz(lv2), la);
-            const ff su = ff_sqrt(ffv(r1));
-            const ff3 yl = ff3_add(ff3_add(ff3v(la), ff3_scale(le1, ff_mul(su, two_sum(1.0f, -r2)))),
-                                   ff3_scale(le2, ff_mul(su, r2)));
-            // (y - x) first: both lie on their planes, so a small surface-to-light gap keeps its
-            // digits; subtracting the rounded offset origin would not. The light sample only
-            // weights this vertex (nothing of it carries to the next bounce), so once the
-            // difference is formed in double-float its length, direction and cosines are FP32:
-            // relative errors ~1e-7 against the 1e-4 bound.
-            const float3 dv = ff3_f(ff3_sub(ff3_sub(yl, x), ff3_scale(nrm, s.eps)));
-            const float d2 = fdot3(dv, dv);
-            const float inv_dist = __fdiv_rn(1.0f, __fsqrt_rn(d2));
-            const float3 wi = mk3(__fmul_rn(dv.x, inv_dist), __fmul_rn(dv.y, inv_dist), __fmul_rn(dv.z, inv_dist));
-            const float cos_x = fdot3(ff3_f(nrm), wi);
-            const ff area2 = ff{ln1.z, ln1.w};
-            const ff3 nl = ff3{ff{ln0.x, ln0.y}, ff{ln0.z, ln0.w}, ff{ln1.x, ln1.y}};
-            const float cl = fdot3(ff3_f(nl), wi);
-            const float cos_l = fabsf(cl);
-            if (cos_x > 0.0f && cos_l > 0.0f && d2 > 0.0f) {
-                out.g = cos_x * cos_l / d2 * (0.5f * ff_f(area2)) * static_cast<float>(s.n_emit) * k_inv_pi;
-                // The shadow ray runs from the light sample, lifted by eps along the light's
-                // normal towards the shading side, to just short of the lifted shading point:
-                // neither end's plane (nor a coplanar neighbour) can be crossed.
-                const float side = cl < 0.0f ? s.eps : -s.eps;
-                const ff3 so = ff3_add(yl, ff3_scale(nl, side));
-                out.seg_o = so;
-                out.seg_d = ff3_sub(out.org, so);
-                const float3 sd = ff3_f(out.seg_d);
-                const float sdist = __fsqrt_rn(fdot3(sd, sd));
-                const float inv_s = __fdiv_rn(1.0f, sdist);
-                out.so = ff3_f(so);
-                out.sd = mk3(__fmul_rn(sd.x, inv_s), __fmul_rn(sd.y, inv_s), __fmul_rn(sd.z, inv_s));
-                out.stmax = sdist * (1.0f - 1e-4f);
-                out.light = l;
-                out.nee = true;
-            }
-        }
+    if (s.n_emit == 0 || lt.l == prim) return;
+    const float3 la = xyz(lt.v0);
+    const ff3 le1 = ff3_diff(xyz(lt.v1), la);
+    const ff3 le2 = ff3_diff(xyz(lt.v2), la);
+    const ff su = ff_sqrt(ffv(r1));
+    const ff3 yl = ff3_add(ff3_add(ff3v(la), ff3_scale(le1, ff_mul(su, two_sum(1.0f, -r2)))),
+                           ff3_scale(le2, ff_mul(su, r2)));
+    // (y - x) first: both lie on their planes, so a small surface-to-light gap keeps its
+    // digits; subtracting the rounded offset origin would not. The light sample only
+    // weights this vertex (nothing of it carries to the next bounce), so once the
+    // difference is formed in double-float its length, direction and cosines are FP32:
+    // relative errors ~1e-7 against the 1e-4 bound.
+    const float3 dv = ff3_f(ff3_sub(ff3_sub(yl, x), ff3_scale(nrm, s.eps)));
+    const float d2 = fdot3(dv, dv);
+    const float inv_dist = __fdiv_rn(1.0f, __fsqrt_rn(d2));
+    const float3 wi = mk3(__fmul_rn(dv.x, inv_dist), __fmul_rn(dv.y, inv_dist), __fmul_rn(dv.z, inv_dist));
+    const float cos_x = fdot3(ff3_f(nrm), wi);
+    const ff area2 = ff{lt.v1.w, lt.v2.w};
+    const ff3 nl = ff3{ff{lt.n0.x, lt.n0.y}, ff{lt.n0.z, lt.n0.w}, ff{lt.n1.x, lt.n1.y}};
+    const float cl = fdot3(ff3_f(nl), wi);
+    const float cos_l = fabsf(cl);
+    if (cos_x > 0.0f && cos_l > 0.0f && d2 > 0.0f) {
+        out.g = cos_x * cos_l / d2 * (0.5f * ff_f(area2)) * static_cast<float>(s.n_emit) * k_inv_pi;
+        // The shadow ray runs from the light sample, lifted by eps along the light's
+        // normal towards the shading side, to just short of the lifted shading point:
+        // neither end's plane (nor a coplanar neighbour) can be crossed.
+        const float side = cl < 0.0f ? s.eps : -s.eps;
+        const ff3 so = ff3_add(yl, ff3_scale(nl, side));
+        out.seg_o = so;
+        out.seg_d = ff3_sub(org, so);
+        const float3 sd = ff3_f(out.seg_d);
+        const float sdist = __fsqrt_rn(fdot3(sd, sd));
+        const float inv_s = __fdiv_rn(1.0f, sdist);
+        out.so = ff3_f(so);
+        out.sd = mk3(__fmul_rn(sd.x, inv_s), __fmul_rn(sd.y, inv_s), __fmul_rn(sd.z, inv_s));
+        out.stmax = sdist * (1.0f - 1e-4f);
+        out.light = lt.l;
+        out.nee = true;
     }
-    const float r3 = rng_next(st);
-    const float r4 = rng_next(st);
-    if (want_dir) {
-        // plugin.mm:111-125 in double-float: phi = 2 pi r3, cos = sqrt(1 - r4), sin = sqrt(r4).
-        ff sphi, cphi;
-        ff_sincospi(2.0f * r3, sphi, cphi);
-        const ff cos_t = ff_sqrt(two_sum(1.0f, -r4));
-        const ff sin_t = ff_sqrt(ffv(r4));
-        // v = normalize(cross(w, a)), a = (0,1,0) if |w.x| > 0.9 else (1,0,0)
-        ff3 vv = fabsf(nrm.x.hi) > 0.9f ? ff3{ff_neg(nrm.z), ffv(0.0f), nrm.x} : ff3{ffv(0.0f), nrm.z, ff_neg(nrm.y)};
-        vv = ff3_normalize(vv);
-        const ff3 uu = ff3_cross(nrm, vv);
-        // (uu, vv, nrm) is orthonormal to ~1e-14 and cos^2 + sin^2 = 1, so the direction is a
-        // unit vector to that accuracy without the final normalisation of plugin.mm:124.
-        out.dir = ff3_add(ff3_add(ff3_scale(uu, ff_mul(cphi, sin_t)), ff3_scale(vv, ff_mul(sphi, sin_t))),
-                          ff3_scale(nrm, cos_t));
-    }
+}
+
+// hit: (t, prim, -, -) from the traversal; ro, rd: the double-float ray that found it. The
+// light choice depends only on the path key: its dependent loads (emitter index, then the
+// light triangle and its table entry) start before the hit-point arithmetic so their latency
+// overlaps it.
+__device__ __forceinline__ void shade_vertex(const VertexScene& s, uint32_t key, int prim, float4 /*hit*/,
+                                             const ff3& ro, const ff3& rd, bool want_dir, VertexResult& out) {
+    const VertexRandom r = vertex_random(key);
+    const LightTri lt = load_light(s, r.sel);
+    ff3 x, nrm;
+    vertex_point(s, prim, ro, rd, x, nrm);
+    out.nrm = ff3_f(nrm);
+    out.org = vertex_origin(s, x, nrm);
+    vertex_light(s, prim, lt, r.r1, r.r2, x, nrm, out.org, out);
+    if (want_dir) out.dir = vertex_dir(nrm, r.r3, r.r4);
 }
 
 // First-hit AOVs (plugin.mm:242-249, 301): albedo (emission for emitters), depth, normal.

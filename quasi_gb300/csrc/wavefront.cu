@@ -197,6 +197,7 @@ int Renderer::set_materials(const float* albedo, const float* emission, uint32_t
     if (tri_count && (!albedo || !emission)) return fail(QUASI_ERR_INVALID, "null materials");
     int rc = upload_materials_host(albedo, emission, tri_count);
     if (rc) return rc;
+    bvh_dirty_ = true;  // the emitters' light-sampling records are rebuilt with the hierarchy
     return reset();
 }
 
@@ -303,7 +304,9 @@ int Renderer::render(const Q_render_frame& fr) {
     if (opt_.integrator == QUASI_INTEGRATOR_NEE && (bvh_dirty_ || opt_.rebuild_each_frame)) {
         NvtxRange bvh_range("quasi.lbvh");
         R_TRY(cudaEventRecord(ev_bvh0_, s), "event");
-        R_TRY(bvh_.build(tri_in_.as<float4>(), n_tris_, s, prof_, err_dev_.as<uint32_t>()), "lbvh build");
+        R_TRY(bvh_.build(tri_in_.as<float4>(), n_tris_, emitters_.as<int>(), n_emit_, s, prof_,
+                         err_dev_.as<uint32_t>()),
+              "lbvh build");
         const int levels = opt_.smem_levels ? static_cast<int>(opt_.smem_levels) : k_default_smem_levels;
         R_TRY(bvh_.build_treelet(levels >= 31 ? 0 : (1 << levels) - 1, s, prof_), "treelet");
         R_TRY(cudaEventRecord(ev_bvh1_, s), "event");
@@ -358,7 +361,7 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
 
     const LbvhView bv = bvh_.view();
     const bool wide = opt_.bvh_width != 2;
-    SceneDev sd{tri_in_.as<float4>(), albedo_.as<float4>(), emission_.as<float4>(), emitters_.as<int>(),
+    SceneDev sd{tri_in_.as<float4>(), albedo_.as<float4>(), emission_.as<float4>(),
                 bv.nodes,
                 bv.tris,
                 n_tris_,
@@ -368,7 +371,8 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
                 wide ? nullptr : bv.tree,
                 wide ? 0 : bv.tree_n,
                 wide ? bv.wide : nullptr,
-                bv.tri_nrm};
+                bv.tri_plane,
+                bv.emit_tab};
     const size_t tree_smem = sizeof(float4) * 4 * static_cast<size_t>(sd.tree_n);
     PathDev pd{beta_.as<float4>(),  lpath_.as<float4>(), aov_a_.as<float4>(),
                aov_n_.as<float4>(), ray_ff_.as<float4>(), opt_.record_samples ? sig_.as<uint32_t>() : nullptr};
@@ -442,7 +446,7 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
             int* f_cur = cnt + 2 * D + (k - 1);
             int* f_shadow = cnt + 3 * D + (k - 1);
             const ClosestJob cjob{qcur, hits_.as<float4>(), ray_ff_.as<float4>(), lpath_.as<float4>(),
-                                  DeferList{defer_.as<int2>(), cnt + 4 * D + (k - 1)}};
+                                  DeferList{defer_.as<int2>(), cnt + 4 * D + (k - 1)}, nullptr};
             const ShadowJob sjob{shadow_.as<float4>(), pd, DeferList{defer_.as<int2>(), cnt + 5 * D + (k - 1)}};
             R_TRY(QUASI_LAUNCH(prof_, "trace_closest", s,
                                (kc<<<grid_c, tb, smem_c, s>>>(sd, cjob, c_cur, cap, f_cur, err, st))),
@@ -451,7 +455,7 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
                                (k_fixup<ClosestJob><<<grid_fixup, 128, 0, s>>>(sd, cjob, cnt + 6 * D + (k - 1), err))),
                   "fixup_closest");
             R_TRY(QUASI_LAUNCH(prof_, "shade", s,
-                               (k_shade<<<grid_shade, 256, 0, s>>>(f, sd, pd, k, qcur, hits_.as<float4>(), c_cur, cap, qnext,
+                               (k_shade<<<grid_shade, 256, 0, s>>>(f, sd, pd, k, hits_.as<float4>(), c_cur, cap, qnext,
                                                                   k < D ? c_next : nullptr, shadow_.as<float4>(),
                                                                   c_shadow))),
                   "shade");
@@ -479,11 +483,10 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
 }
 
 SceneDev Renderer_scene_dev(const LbvhView& bv, const DeviceBuffer& tri_in, const DeviceBuffer& albedo,
-                            const DeviceBuffer& emission, const DeviceBuffer& emitters, uint32_t n_tris, uint32_t n_emit,
-                            uint32_t bvh_width) {
-    return SceneDev{tri_in.as<float4>(), albedo.as<float4>(), emission.as<float4>(), emitters.as<int>(), bv.nodes,
-                    bv.tris, n_tris, n_emit, k_refill_lanes, k_trace_steps, nullptr, 0,
-                    bvh_width == 2 ? nullptr : bv.wide, bv.tri_nrm};
+                            const DeviceBuffer& emission, uint32_t n_tris, uint32_t n_emit, uint32_t bvh_width) {
+    return SceneDev{tri_in.as<float4>(), albedo.as<float4>(), emission.as<float4>(), bv.nodes, bv.tris, n_tris, n_emit,
+                    k_refill_lanes, k_trace_steps, nullptr, 0, bvh_width == 2 ? nullptr : bv.wide, bv.tri_plane,
+                    bv.emit_tab};
 }
 
 FrameParams Renderer::frame_params(uint32_t spp, uint32_t slots, uint32_t tiles_x) const {
@@ -519,7 +522,7 @@ int Renderer::render_megakernel(cudaStream_t s, uint32_t spp) {
     R_TRY(cudaMemsetAsync(counters_.ptr, 0, sizeof(int) * (waves + 2), s), "memset");
     R_TRY(cudaMemsetAsync(stats_dev_.ptr, 0, sizeof(unsigned long long) * 4, s), "memset");
     R_TRY(cudaMemsetAsync(stats_dev_.as<unsigned long long>() + 5, 0, sizeof(unsigned long long) * 2, s), "memset");
-    const SceneDev sd = Renderer_scene_dev(bvh_.view(), tri_in_, albedo_, emission_, emitters_, n_tris_, n_emit_,
+    const SceneDev sd = Renderer_scene_dev(bvh_.view(), tri_in_, albedo_, emission_, n_tris_, n_emit_,
                                            opt_.bvh_width);
     PathDev pd{beta_.as<float4>(),  lpath_.as<float4>(), aov_a_.as<float4>(),
                aov_n_.as<float4>(), ray_ff_.as<float4>(), opt_.record_samples ? sig_.as<uint32_t>() : nullptr};
@@ -573,7 +576,9 @@ int Renderer::backward(const float* grad_image, uint32_t spp, uint32_t sample_ba
     if (width_ == 0 || height_ == 0) return fail(QUASI_ERR_STATE, "render a frame before backward");
     cudaStream_t s = stream_;
     if (bvh_dirty_) {
-        R_TRY(bvh_.build(tri_in_.as<float4>(), n_tris_, s, prof_, err_dev_.as<uint32_t>()), "lbvh build");
+        R_TRY(bvh_.build(tri_in_.as<float4>(), n_tris_, emitters_.as<int>(), n_emit_, s, prof_,
+                         err_dev_.as<uint32_t>()),
+              "lbvh build");
         bvh_dirty_ = false;
     }
     R_TRY(cudaMemsetAsync(grad_albedo, 0, sizeof(float) * 3ull * n_tris_, s), "memset");
@@ -591,7 +596,7 @@ int Renderer::backward(const float* grad_image, uint32_t spp, uint32_t sample_ba
     f.wave_spp = spp;
     f.sample_base = sample_base;
     f.wave_offset = 0;
-    const SceneDev sd = Renderer_scene_dev(bvh_.view(), tri_in_, albedo_, emission_, emitters_, n_tris_, n_emit_,
+    const SceneDev sd = Renderer_scene_dev(bvh_.view(), tri_in_, albedo_, emission_, n_tris_, n_emit_,
                                            opt_.bvh_width);
     int occ = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjoint, 128, 0);
@@ -667,7 +672,9 @@ int Renderer::read_samples(float* radiance, uint32_t* signatures) {
 int Renderer::read_bvh(uint32_t* morton, uint32_t* order, int32_t* children, float* boxes, float* bounds) {
     if (!has_scene_) return fail(QUASI_ERR_STATE, "no scene");
     if (bvh_dirty_) {
-        R_TRY(bvh_.build(tri_in_.as<float4>(), n_tris_, stream_, prof_, err_dev_.as<uint32_t>()), "lbvh build");
+        R_TRY(bvh_.build(tri_in_.as<float4>(), n_tris_, emitters_.as<int>(), n_emit_, stream_, prof_,
+                         err_dev_.as<uint32_t>()),
+              "lbvh build");
         bvh_dirty_ = false;
     }
     R_TRY(bvh_.read(morton, order, children, boxes, bounds, stream_), "read bvh");
@@ -677,7 +684,9 @@ int Renderer::read_bvh(uint32_t* morton, uint32_t* order, int32_t* children, flo
 int Renderer::read_wide_bvh(uint32_t* words) {
     if (!has_scene_) return fail(QUASI_ERR_STATE, "no scene");
     if (bvh_dirty_) {
-        R_TRY(bvh_.build(tri_in_.as<float4>(), n_tris_, stream_, prof_, err_dev_.as<uint32_t>()), "lbvh build");
+        R_TRY(bvh_.build(tri_in_.as<float4>(), n_tris_, emitters_.as<int>(), n_emit_, stream_, prof_,
+                         err_dev_.as<uint32_t>()),
+              "lbvh build");
         bvh_dirty_ = false;
     }
     R_TRY(bvh_.read_wide(words, stream_), "read wide bvh");

@@ -63,6 +63,8 @@ __global__ void __launch_bounds__(256, trace_min_blocks(MODE)) k_trace_closest(S
                                                        const int* __restrict__ count, int capacity,
                                                        int* __restrict__ fetch, uint32_t* __restrict__ err,
                                                        unsigned long long* __restrict__ stats) {
+    __shared__ int s_pid[256];
+    job.slot_pid = s_pid;
     const int n = min(*count, capacity);
     uint32_t e = 0;
     TraceCounters c;
@@ -145,16 +147,8 @@ __global__ void k_tally(const int* __restrict__ counters, uint32_t waves, uint32
     if (threadIdx.x == 0) stats[4] += sum;
 }
 
-// Minimum resident 256-thread blocks per SM asked of the compiler for k_shade (a register
-// cap). Before the shading table it took 141 registers uncapped and the 1080p frame's
-// shading cost 138 ms; 2 blocks (128 registers) or 4 (64, with spills) cost 101 ms on
-// GB300. Now it takes 119 registers at 2 blocks (50 ms); 3 blocks (85 registers) cost 53 ms.
-#ifndef QUASI_SHADE_MIN_BLOCKS
-#define QUASI_SHADE_MIN_BLOCKS 2
-#endif
-
 __global__ void __launch_bounds__(256, QUASI_SHADE_MIN_BLOCKS) k_shade(FrameParams f, SceneDev s, PathDev p, uint32_t bounce,
-                                               const float4* __restrict__ q, const float4* __restrict__ hits,
+                                               const float4* __restrict__ hits,
                                                const int* __restrict__ count, int capacity, float4* __restrict__ next_q,
                                                int* __restrict__ next_count, float4* __restrict__ shadow_q,
                                                int* __restrict__ shadow_count) {
@@ -163,20 +157,15 @@ __global__ void __launch_bounds__(256, QUASI_SHADE_MIN_BLOCKS) k_shade(FramePara
     const int stride = gridDim.x * blockDim.x;
     for (int base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; base < n; base += stride) {
         const int i = base + lane;
-        HitShade o;
-        o.shadow = o.next = false;
-        int pid = 0, prim = -1;
+        int pid = 0;
+        float4 h = make_float4(0.f, __int_as_float(-1), 0.f, 0.f);
         if (i < n) {
-            const float4 h = hits[i];
-            pid = __float_as_int(q[2 * i].w);
-            prim = __float_as_int(h.y);
-            if (prim < 0) {
-                if (p.sig) p.sig[pid] = sig_mix(p.sig[pid], k_sig_miss);
-            } else {
-                shade_hit(f, s, p, bounce, pid, static_cast<uint32_t>(pid), h, o);
-            }
+            h = hits[i];
+            pid = __float_as_int(h.z);
+            if (__float_as_int(h.y) < 0 && p.sig) p.sig[pid] = sig_mix(p.sig[pid], k_sig_miss);
         }
-        enqueue_shaded(i < n && prim >= 0, pid, prim, o, shadow_q, shadow_count, next_q, next_count);
+        shade_and_enqueue(i < n && __float_as_int(h.y) >= 0, f, s, p, bounce, pid, static_cast<uint32_t>(pid), h,
+                          shadow_q, shadow_count, next_q, next_count);
     }
 }
 
