@@ -344,7 +344,9 @@ int BatchRenderer::record_frame(cudaStream_t s, uint32_t& launches) {
     auto km = stats ? k_batch_megakernel<true> : k_batch_megakernel<false>;
     const int grid_c = grid_c_, grid_s = grid_s_, grid_m = grid_m_;
     const int grid_shade = sm * 8;
-    const int grid_fixup = sm * 4;
+    int occ_f = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, k_batch_fixup<ClosestJob>, 128, 0);
+    const int grid_fixup = sm * std::max(occ_f, 1);
     const int cap = static_cast<int>(wave_capacity_);
     for (size_t w = 0; w < waves_.size(); ++w) {
         const Wave& wv = waves_[w];
@@ -369,8 +371,10 @@ int BatchRenderer::record_frame(cudaStream_t s, uint32_t& launches) {
                 int* f_cur = cnt + 2 * D + (k - 1);
                 int* f_shadow = cnt + 3 * D + (k - 1);
                 const ClosestJob cjob{qcur, hits_.as<float4>(), ray_ff_.as<float4>(), lpath_.as<float4>(),
-                                      DeferList{defer_.as<int2>(), cnt + 4 * D + (k - 1)}, nullptr};
-                const ShadowJob sjob{shadow_.as<float4>(), pd, DeferList{defer_.as<int2>(), cnt + 5 * D + (k - 1)}};
+                                      DeferList{defer_.as<int2>(), cnt + 4 * D + (k - 1), cnt + 8 * D + (k - 1), cap},
+                                      nullptr};
+                const ShadowJob sjob{shadow_.as<float4>(), pd,
+                                     DeferList{defer_.as<int2>(), cnt + 5 * D + (k - 1), cnt + 9 * D + (k - 1), cap}};
                 B_TRY(QUASI_LAUNCH(prof_, "batch_trace_closest", s,
                                    (kc<<<grid_c, tb, smem_c_, s>>>(table, meta, cjob, c_cur, cap, chunk, refill, f_cur, err,
                                                                    st))),

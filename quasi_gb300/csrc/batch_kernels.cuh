@@ -210,47 +210,23 @@ __global__ void __launch_bounds__(256, WIDE ? QUASI_WIDE_MIN_BLOCKS : 1) k_batch
 
 // Completes the rays a batch trace kernel deferred (robust.cuh) with each ray's scene:
 // re-decides its recorded candidate exactly against its certain result, or re-traces a ray
-// that met more than one over the scene's binary LBVH. One entry per thread.
+// that met more than one over the scene's 8-wide records or binary LBVH (resolve_deferred).
 template <class Job>
 __global__ void __launch_bounds__(128) k_batch_fixup(const BatchSceneDev* __restrict__ scenes,
                                                      const uint2* __restrict__ meta, Job job,
                                                      int* __restrict__ fetch, uint32_t* __restrict__ err) {
     constexpr bool any = std::is_same<Job, ShadowJob>::value;
-    const int lane = threadIdx.x & 31;
-    const int n = *job.deferred.count;
     uint32_t e = 0;
-    TraceCounters cnt;
-    while (true) {
-        int base = 0;
-        if (lane == 0) base = atomicAdd(fetch, 32);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n) break;
-        const int k = base + lane;
-        if (k < n) {
-            const int2 en = job.deferred.list[k];
-            const int i = en.x;
-            const SceneDev& s = scenes[meta[job.pid(i)].x].s;
-            HitBest b;
-            if (en.y == k_undec_many) {
-                float3 o, d;
-                float tmax;
-                int exclude;
-                job.load(i, o, d, tmax, exclude);
-                if (s.wide) {
-                    b = trace_wide_exact<any>(s.wide, s.tris, s.tri_in, s.n_tris, o, d, tmax, exclude, job.exact(i), e);
-                } else {
-                    const RayInv r = make_ray(o, d, s.n_tris ? scene_box_pad(s.nodes) : 0.0f);
-                    b = trace_bvh<any, false, false, true>(s.nodes, s.tris, s.tri_in, s.n_tris, r, tmax, exclude, e,
-                                                           cnt, job.exact(i));
-                }
-            } else {
-                b = job.partial(i);
-                redecide<any>(s.tri_in, job.exact(i), en.y, b);
-            }
-            b.undec = k_undec_none;
-            job.store(i, trace_result(b));
-        }
-    }
+    auto scene = [&](int i) -> const SceneDev& { return scenes[meta[job.pid(i)].x].s; };
+    auto retrace = [&](int i, float3 o, float3 d, float tmax, int exclude) {
+        const SceneDev& s = scene(i);
+        if (s.wide) return trace_wide_exact<any>(s.wide, s.tris, s.tri_in, s.n_tris, o, d, tmax, exclude, job.exact(i), e);
+        TraceCounters cnt;
+        const RayInv r = make_ray(o, d, s.n_tris ? scene_box_pad(s.nodes) : 0.0f);
+        return trace_bvh<any, false, false, true>(s.nodes, s.tris, s.tri_in, s.n_tris, r, tmax, exclude, e, cnt,
+                                                  job.exact(i));
+    };
+    resolve_deferred<any>(job, [&](int i) { return scene(i).tri_in; }, job.deferred, fetch, retrace);
     if (e) atomicOr(err, e);
 }
 
@@ -399,9 +375,10 @@ __global__ void __launch_bounds__(128) k_batch_adjoint(const BatchSceneDev* __re
 }
 
 // Per-wave counters of the wavefront form, k_batch_counters_per_bounce per bounce: queue
-// lengths [0, 2D), trace fetch counters [2D, 4D), deferred rays [4D, 6D), fixup fetch
-// counters [6D, 8D).
-constexpr uint32_t k_batch_counters_per_bounce = 8;
+// lengths [0, 2D), trace fetch counters [2D, 4D), rays deferred with one undecided
+// candidate [4D, 6D), fixup fetch counters [6D, 8D), rays deferred to be re-traced whole
+// [8D, 10D).
+constexpr uint32_t k_batch_counters_per_bounce = 10;
 
 // Adds the frame's closest-hit and shadow queue lengths to stats[5] and stats[6] and the
 // rays re-traced by the fixup kernels to stats[8]. One warp.
@@ -414,7 +391,8 @@ __global__ void k_batch_tally(const int* __restrict__ counters, uint32_t waves, 
         const unsigned long long v = static_cast<unsigned long long>(max(c[k], 0));
         if (k < depth) closest += v;
         else shadow += v;
-        redecided += static_cast<unsigned long long>(max(c[4 * depth + k], 0));
+        redecided += static_cast<unsigned long long>(max(c[4 * depth + k], 0)) +
+                     static_cast<unsigned long long>(max(c[8 * depth + k], 0));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {

@@ -4,7 +4,7 @@
 // from error-free transformations that run at FP32 rate: Knuth's TwoSum, Dekker's
 // FastTwoSum, TwoProd through a fused multiply-add, and Dekker's (1971) double-length
 // add / multiply / divide / square root as organised in the QD library (Hida, Li and
-// Bailey, 2001). sin and cos come from their Taylor series after reduction to |x| <= pi/4.
+// Bailey, 2001). sin and cos come from a table of 33 angles and short Taylor series.
 //
 // Why: FP32 coordinates near 1.0 carry 6e-8 of absolute rounding. A path that bounces in a
 // corner (segments of 1e-4) turns that into 1e-3 of relative error in its radiance, far
@@ -67,59 +67,102 @@ __device__ __forceinline__ ff ff_mul(ff a, float b) {
     return fast_two_sum(p.hi, p.lo);
 }
 
+// a + b for a float b (one TwoSum fewer than ff_add; the same ~2^-48 relative accuracy).
+__device__ __forceinline__ ff ff_add(ff a, float b) {
+    ff s = two_sum(a.hi, b);
+    s.lo = __fadd_rn(s.lo, a.lo);
+    return fast_two_sum(s.hi, s.lo);
+}
+
+// Three quotient digits, each the running remainder times one float reciprocal of b.hi; the
+// exact remainders absorb the reciprocal's rounding, so the result keeps ~2^-47 relative
+// accuracy with one reciprocal instead of three divisions.
 __device__ __forceinline__ ff ff_div(ff a, ff b) {
-    const float q1 = __fdiv_rn(a.hi, b.hi);
+    const float rb = __frcp_rn(b.hi);
+    const float q1 = __fmul_rn(a.hi, rb);
     ff r = ff_sub(a, ff_mul(b, q1));
-    const float q2 = __fdiv_rn(r.hi, b.hi);
+    const float q2 = __fmul_rn(r.hi, rb);
     r = ff_sub(r, ff_mul(b, q2));
-    const float q3 = __fdiv_rn(r.hi, b.hi);
-    return ff_add(fast_two_sum(q1, q2), ffv(q3));
+    const float q3 = __fmul_rn(r.hi, rb);
+    return ff_add(fast_two_sum(q1, q2), q3);
 }
 
 __device__ __forceinline__ ff ff_sqrt(ff a) {
     if (!(a.hi > 0.0f)) return ff{0.0f, 0.0f};
     const float s = __fsqrt_rn(a.hi);
     const ff r = ff_sub(a, two_prod(s, s));
-    return fast_two_sum(s, __fdiv_rn(r.hi, __fmul_rn(2.0f, s)));
+    return fast_two_sum(s, __fmul_rn(r.hi, __frcp_rn(__fmul_rn(2.0f, s))));
 }
 
 __device__ __forceinline__ float ff_f(ff a) { return __fadd_rn(a.hi, a.lo); }
 
-// sin(pi x) and cos(pi x) for a float x: x = k/2 + y with |y| <= 1/4 exactly, then Taylor
-// series of sin and cos at pi*y to degree 15 and 14: the first omitted terms are below
-// 5e-17 and 1.1e-15 for |pi y| <= pi/4, under the ~1e-14 of double-float arithmetic.
+// sin(pi j / 128) and cos(pi j / 128) for j = 0..32 as double-float pairs
+// (sin.hi, sin.lo, cos.hi, cos.lo): the exact values rounded to ~48 bits, computed from their
+// Taylor series in 60-digit decimal arithmetic (tests/test_ffmath.py recomputes them).
+namespace {
+__device__ const float k_sincospi_tab[33][4] = {
+    {0.0f, 0.0f, 1.0f, 0.0f},
+    {0.024541229009628296f, -4.867160008359406e-10f, 0.99969881772995f, 9.66254298795377e-10f},
+    {0.049067676067352295f, -1.7399343077428853e-09f, 0.9987954497337341f, 6.471438052102485e-09f},
+    {0.0735645666718483f, -3.0721809540779077e-09f, 0.9972904324531555f, 2.4225535355526517e-08f},
+    {0.0980171412229538f, -8.933931927579408e-10f, 0.9951847195625305f, 7.109666189109021e-09f},
+    {0.12241067737340927f, -2.1741930478214044e-09f, 0.9924795627593994f, -2.8160689780065695e-08f},
+    {0.1467304676771164f, 6.778245520422388e-09f, 0.9891765117645264f, -1.7997453527485163e-09f},
+    {0.1709618866443634f, 2.115937869362483e-09f, 0.9852776527404785f, -1.0351537405028921e-08f},
+    {0.19509032368659973f, -1.670471427850373e-09f, 0.9807852506637573f, 2.9739473106360492e-08f},
+    {0.21910123527050018f, 4.88636953122068e-09f, 0.9757021069526672f, 2.3085862110860944e-08f},
+    {0.24298018217086792f, -2.267604104488896e-09f, 0.9700312614440918f, -8.249547711614014e-09f},
+    {0.2667127549648285f, 2.5100699296842777e-09f, 0.9637760519981384f, 1.3797301079421231e-08f},
+    {0.290284663438797f, 1.3815665056426951e-08f, 0.9569403529167175f, -1.7184508038781132e-08f},
+    {0.3136817514896393f, -1.1090747875641682e-08f, 0.949528157711029f, 2.288200739997137e-08f},
+    {0.3368898630142212f, -9.622000973763534e-09f, 0.9415440559387207f, 9.244300436250796e-09f},
+    {0.3598950505256653f, -1.3990677061315182e-08f, 0.9329928159713745f, -1.7136635221959295e-08f},
+    {0.3826834261417389f, 6.2233507236442165e-09f, 0.9238795042037964f, 2.830748968563057e-08f},
+    {0.40524131059646606f, 3.4085239075665186e-09f, 0.91420978307724f, -2.7373708633149363e-08f},
+    {0.4275550842285156f, 9.201766459909777e-09f, 0.903989315032959f, -2.1909515979245953e-08f},
+    {0.4496113359928131f, -6.338206404166158e-09f, 0.89322429895401f, 2.241505203670613e-09f},
+    {0.4713967442512512f, -7.425253745196869e-09f, 0.8819212913513184f, -2.7002963420841297e-08f},
+    {0.49289819598197937f, -3.75219544324068e-09f, 0.8700869679450989f, 2.3163613249721493e-08f},
+    {0.5141027569770813f, -1.2783859304477119e-08f, 0.8577286005020142f, 9.498258179974073e-09f},
+    {0.5349976420402527f, -2.2153155754267573e-08f, 0.8448535799980164f, -1.4748309240530943e-08f},
+    {0.5555702447891235f, -1.1769521357507529e-08f, 0.8314695954322815f, 1.687026340846387e-08f},
+    {0.5758081674575806f, 2.396026488327152e-08f, 0.8175848126411438f, 5.104399125599457e-10f},
+    {0.5956993103027344f, -5.810301129116624e-09f, 0.803207516670227f, 1.4810417781063734e-08f},
+    {0.6152315735816956f, 1.6998932039768988e-08f, 0.7883464097976685f, 1.7828938325692434e-08f},
+    {0.6343932747840881f, 9.37955757507325e-09f, 0.7730104327201843f, 2.0642552556182636e-08f},
+    {0.6531728506088257f, -7.655049039101414e-09f, 0.7572088241577148f, 2.2348769945779168e-08f},
+    {0.6715589761734009f, -2.1326382437791835e-08f, 0.7409511208534241f, 4.501535144640911e-09f},
+    {0.6895405650138855f, -2.027681844651852e-08f, 0.7242470979690552f, -1.5017588950172467e-08f},
+    {0.7071067690849304f, 1.2101617485882343e-08f, 0.7071067690849304f, 1.2101617485882343e-08f},
+};
+}  // namespace
+
+// sin(pi x) and cos(pi x) for a float x: x = k/2 + j/128 + z exactly, with |j| <= 32 and
+// |z| <= 1/256; sin and cos of pi z from their Taylor series (degree 5 and 6: the first
+// omitted terms are below 1e-16 of the result for |pi z| <= pi/256, the double-float terms
+// are the ones above 1e-9), then the angle-sum formulas with the table entry for |j| and the
+// quadrant k.
 __device__ __forceinline__ void ff_sincospi(float x, ff& s, ff& c) {
     const float k = rintf(__fmul_rn(2.0f, x));
-    const float y = __fsub_rn(x, __fmul_rn(0.5f, k));
+    const float y = __fsub_rn(x, __fmul_rn(0.5f, k));          // |y| <= 1/4, exact
     const int q = static_cast<int>(k) & 3;
-    const ff t = ff_mul(ff{3.14159274101257324f, -8.742277657347586e-08f}, y);
-    const ff t2 = ff_mul(t, t);
-    // (-1)^k / (2k+1)! and (-1)^k / (2k)!, as hi + lo float pairs, highest order first.
-    const float sin_c[8][2] = {{-7.647163609812713e-13f, -1.2200710471178288e-20f},
-                               {1.6059044372074283e-10f, -5.352526511562726e-18f},
-                               {-2.5052107943679403e-08f, -4.4176230446483665e-16f},
-                               {2.7557318844628753e-06f, 3.793571224297229e-14f},
-                               {-0.00019841270113829523f, 2.725596874933456e-12f},
-                               {0.008333333767950535f, -4.34617203337595e-10f},
-                               {-0.1666666716337204f, 4.967053879312289e-09f},
-                               {1.0f, 0.0f}};
-    const float cos_c[8][2] = {{-1.147074536050896e-11f, -2.372207689231238e-19f},
-                               {2.0876755879584152e-09f, 1.1082839809204342e-16f},
-                               {-2.755731998149713e-07f, 7.575112209051195e-15f},
-                               {2.4801587642286904e-05f, -3.40699609366682e-13f},
-                               {-0.0013888889225199819f, 3.3631094437103215e-11f},
-                               {0.0416666679084301f, -1.2417634698280722e-09f},
-                               {-0.5f, 0.0f},
-                               {1.0f, 0.0f}};
-    ff ps = ff{sin_c[0][0], sin_c[0][1]};
-    ff pc = ff{cos_c[0][0], cos_c[0][1]};
-#pragma unroll
-    for (int i = 1; i < 8; ++i) {
-        ps = ff_add(ff_mul(ps, t2), ff{sin_c[i][0], sin_c[i][1]});
-        pc = ff_add(ff_mul(pc, t2), ff{cos_c[i][0], cos_c[i][1]});
-    }
-    const ff sv = ff_mul(ps, t);
-    const ff cv = pc;
+    const float jf = rintf(__fmul_rn(128.0f, y));
+    const float z = __fsub_rn(y, __fmul_rn(jf, 0.0078125f));   // |z| <= 1/256, exact (Sterbenz)
+    const ff b = ff_mul(ff{3.14159274101257324f, -8.742277657347586e-08f}, z);
+    const ff b2 = ff_mul(b, b);
+    const float f2 = b2.hi;
+    // sin b = b + b^3 (-1/6 + b^2 (1/120 - b^2 / 5040)), cos b = 1 + b^2 (-1/2 + b^2 (1/24 - b^2 / 720))
+    const ff ps = ff_add(ff{-0.1666666716337204f, 4.967053879312289e-09f},
+                         __fmul_rn(f2, __fmaf_rn(f2, -1.984127e-4f, 8.333333e-3f)));
+    const ff pc = ff_add(ffv(-0.5f), __fmul_rn(f2, __fmaf_rn(f2, -1.3888889e-3f, 4.1666668e-2f)));
+    const ff sb = ff_add(b, ff_mul(ff_mul(b, b2), ps));
+    const ff cb = ff_add(ffv(1.0f), ff_mul(b2, pc));
+    const int j = abs(static_cast<int>(jf));
+    ff sa{k_sincospi_tab[j][0], k_sincospi_tab[j][1]};
+    const ff ca{k_sincospi_tab[j][2], k_sincospi_tab[j][3]};
+    if (jf < 0.0f) sa = ff_neg(sa);
+    const ff sv = ff_add(ff_mul(sa, cb), ff_mul(ca, sb));
+    const ff cv = ff_sub(ff_mul(ca, cb), ff_mul(sa, sb));
     switch (q) {
         case 0: s = sv; c = cv; break;
         case 1: s = cv; c = ff_neg(sv); break;

@@ -69,12 +69,6 @@ struct PathDev {
 
 // Rays a fast trace kernel could not decide for certain (robust.cuh): entries (ray index,
 // undecided candidate) for the fixup kernel.
-struct DeferList {
-    int2* list;
-    int* count;
-    __device__ __forceinline__ void push(int i, int undec) const { list[atomicAdd(count, 1)] = make_int2(i, undec); }
-};
-
 // Pixel slots are ordered in 8x4 tiles so a warp's camera rays cover a compact patch.
 __device__ __forceinline__ void slot_to_xy(uint32_t slot, uint32_t tiles_x, uint32_t& x, uint32_t& y) {
     const uint32_t tile = slot >> 5, in = slot & 31u;

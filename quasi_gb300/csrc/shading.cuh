@@ -113,21 +113,35 @@ __device__ __forceinline__ ff3 vertex_origin(const VertexScene& s, const ff3& x,
     return ff3_add(x, ff3_scale(nrm, s.eps));
 }
 
-// Cosine-weighted continuation direction about nrm (plugin.mm:111-125) in double-float:
-// phi = 2 pi r3, cos = sqrt(1 - r4), sin = sqrt(r4).
+// Cosine-weighted continuation direction about n = nrm (plugin.mm:111-125) in double-float:
+// phi = 2 pi r3, cos = sqrt(1 - r4), sin = sqrt(r4), in the basis (u, v, n) with
+// v = normalize(cross(n, a)), a = (0,1,0) if |n.x| > 0.9 else (1,0,0), u = cross(n, v).
+// With c = cross(n, a): v = c / |c| and u = cross(n, c) / |c|, whose components are single
+// products (|c|^2 is the sum of the other two squares), so
+//   dir = (cross(n, c) cos(phi) + c sin(phi)) sin / |c| + n cos
+// with one division and no normalised basis vectors. The basis is orthonormal to ~1e-14 and
+// cos^2 + sin^2 = 1, so dir is a unit vector to that accuracy without the final
+// normalisation of plugin.mm:124.
 __device__ __forceinline__ ff3 vertex_dir(const ff3& nrm, float r3, float r4) {
     ff sphi, cphi;
     ff_sincospi(2.0f * r3, sphi, cphi);
     const ff cos_t = ff_sqrt(two_sum(1.0f, -r4));
     const ff sin_t = ff_sqrt(ffv(r4));
-    // v = normalize(cross(w, a)), a = (0,1,0) if |w.x| > 0.9 else (1,0,0)
-    ff3 vv = fabsf(nrm.x.hi) > 0.9f ? ff3{ff_neg(nrm.z), ffv(0.0f), nrm.x} : ff3{ffv(0.0f), nrm.z, ff_neg(nrm.y)};
-    vv = ff3_normalize(vv);
-    const ff3 uu = ff3_cross(nrm, vv);
-    // (uu, vv, nrm) is orthonormal to ~1e-14 and cos^2 + sin^2 = 1, so the direction is a
-    // unit vector to that accuracy without the final normalisation of plugin.mm:124.
-    return ff3_add(ff3_add(ff3_scale(uu, ff_mul(cphi, sin_t)), ff3_scale(vv, ff_mul(sphi, sin_t))),
-                   ff3_scale(nrm, cos_t));
+    const ff &x = nrm.x, &y = nrm.y, &z = nrm.z;
+    ff3 c, nc;  // c = cross(n, a), nc = cross(n, c)
+    ff cc;      // |c|^2
+    if (fabsf(x.hi) > 0.9f) {
+        cc = ff_add(ff_mul(x, x), ff_mul(z, z));
+        c = ff3{ff_neg(z), ffv(0.0f), x};
+        nc = ff3{ff_mul(x, y), ff_neg(cc), ff_mul(y, z)};
+    } else {
+        cc = ff_add(ff_mul(y, y), ff_mul(z, z));
+        c = ff3{ffv(0.0f), z, ff_neg(y)};
+        nc = ff3{ff_neg(cc), ff_mul(x, y), ff_mul(x, z)};
+    }
+    const ff g = ff_div(sin_t, ff_sqrt(cc));
+    const ff wu = ff_mul(cphi, g), wv = ff_mul(sphi, g);
+    return ff3_add(ff3_add(ff3_scale(nc, wu), ff3_scale(c, wv)), ff3_scale(nrm, cos_t));
 }
 
 // The NEE sample of a vertex at x (normal nrm, continuation origin org) towards the light
@@ -144,12 +158,15 @@ __device__ __forceinline__ void vertex_light(const VertexScene& s, int prim, con
     const ff su = ff_sqrt(ffv(r1));
     const ff3 yl = ff3_add(ff3_add(ff3v(la), ff3_scale(le1, ff_mul(su, two_sum(1.0f, -r2)))),
                            ff3_scale(le2, ff_mul(su, r2)));
-    // (y - x) first: both lie on their planes, so a small surface-to-light gap keeps its
-    // digits; subtracting the rounded offset origin would not. The light sample only
-    // weights this vertex (nothing of it carries to the next bounce), so once the
-    // difference is formed in double-float its length, direction and cosines are FP32:
-    // relative errors ~1e-7 against the 1e-4 bound.
-    const float3 dv = ff3_f(ff3_sub(ff3_sub(yl, x), ff3_scale(nrm, s.eps)));
+    // (y - x) first, in double-float: both lie on their planes, so a small surface-to-light
+    // gap keeps its digits; subtracting the rounded offset origin would not. The light sample
+    // only weights this vertex (nothing of it carries to the next bounce), so once that
+    // difference is formed the eps offset, length, direction and cosines are FP32: relative
+    // errors ~1e-7 against the 1e-4 bound.
+    const float3 d0 = ff3_f(ff3_sub(yl, x));
+    const float3 nf = ff3_f(nrm);
+    const float3 dv = mk3(__fsub_rn(d0.x, __fmul_rn(s.eps, nf.x)), __fsub_rn(d0.y, __fmul_rn(s.eps, nf.y)),
+                          __fsub_rn(d0.z, __fmul_rn(s.eps, nf.z)));
     const float d2 = fdot3(dv, dv);
     const float inv_dist = __fdiv_rn(1.0f, __fsqrt_rn(d2));
     const float3 wi = mk3(__fmul_rn(dv.x, inv_dist), __fmul_rn(dv.y, inv_dist), __fmul_rn(dv.z, inv_dist));

@@ -318,6 +318,46 @@ __device__ __forceinline__ HitBest trace_bvh(const float4* __restrict__ nodes, c
 
 // Hands one finished ray to the job: a ray with an undecided candidate goes to the fixup
 // list (with its certain result), others store their final result.
+// The rays a trace kernel leaves to its fixup kernel, as (ray, recorded candidate) pairs: rays
+// with one undecided candidate from the front of the list, rays to re-trace whole
+// (k_undec_many) from the back, so the fixup kernel can spread the long re-traces one per
+// warp.
+struct DeferList {
+    int2* list;
+    int* count;       // entries at the front
+    int* count_many;  // entries at the back
+    int capacity;     // entries the list holds (one per ray of the launch)
+    __device__ __forceinline__ void push(int i, int undec) const {
+        if (undec == k_undec_many)
+            list[capacity - 1 - atomicAdd(count_many, 1)] = make_int2(i, undec);
+        else
+            list[atomicAdd(count, 1)] = make_int2(i, undec);
+    }
+    // Entry of lane `lane` in chunk c of the fixup order (n_many re-traces, n_single single
+    // re-decisions): while re-traces last, lane 0 of each chunk takes one and lanes 1..31 take
+    // single entries; later chunks hold 32 single entries. Returns false past the end.
+    __device__ __forceinline__ bool entry(int c, int lane, int n_many, int n_single, int2& e) const {
+        int k;
+        if (c < n_many) {
+            if (lane == 0) {
+                e = list[capacity - 1 - c];
+                return true;
+            }
+            k = 31 * c + lane - 1;
+        } else {
+            k = 31 * n_many + 32 * (c - n_many) + lane;
+        }
+        if (k >= n_single) return false;
+        e = list[k];
+        return true;
+    }
+    // Chunks of the fixup order.
+    __device__ __forceinline__ static int chunks(int n_many, int n_single) {
+        const int rest = n_single - 31 * n_many;
+        return n_many + (rest > 0 ? (rest + 31) / 32 : 0);
+    }
+};
+
 template <class Job>
 __device__ __forceinline__ void finish_ray(Job& job, int i, const TraceResult& res) {
     if (res.undec != k_undec_none)
@@ -405,25 +445,29 @@ __device__ __forceinline__ void trace_persistent(Job& job, const float4* __restr
     }
 }
 
-// Completes the rays a fast trace kernel deferred: entry k of `list` is (ray i, its
-// undecided candidate). One entry per thread, 32 entries per warp and atomic, so the exact
-// re-decisions run with the lanes in step. A candidate is re-decided against the ray's
-// certain result (job.partial(i)); a ray that met more than one is re-traced whole with
-// inline re-decisions by `retrace(o, d, tmax, exclude, exact)` (over the 8-wide records or
-// the binary LBVH). Job supplies load, store, partial(i) and exact(i).
-template <bool ANY, class Job, class Retrace>
-__device__ __forceinline__ void resolve_deferred(Job& job, const float4* __restrict__ tri_in,
-                                                 const int2* __restrict__ list, int n, int* __restrict__ fetch,
-                                                 const Retrace& retrace) {
+// Completes the rays a trace kernel deferred. List entries are (ray i, its undecided
+// candidate); each warp takes one chunk of 32 per atomic (DeferList::entry): a ray to
+// re-trace whole in lane 0 while they last, single re-decisions in the other lanes. A
+// re-trace makes its own exact re-decisions one lane at a time, so spreading re-traces one
+// per warp keeps those from queueing behind each other. A candidate is re-decided against
+// the ray's certain result (job.partial(i)); a ray that met more than one is re-traced whole
+// with inline re-decisions by `retrace(i, o, d, tmax, exclude)` (over the 8-wide records or
+// the binary LBVH). Job supplies load, store, partial(i) and exact(i); tri_in(i) gives the
+// original triangles of ray i's scene.
+template <bool ANY, class Job, class TriIn, class Retrace>
+__device__ __forceinline__ void resolve_deferred(Job& job, const TriIn& tri_in, const DeferList& dl,
+                                                 int* __restrict__ fetch, const Retrace& retrace) {
     const int lane = threadIdx.x & 31;
+    const int n_many = *dl.count_many;
+    const int n_single = *dl.count;
+    const int n_chunks = DeferList::chunks(n_many, n_single);
     while (true) {
-        int base = 0;
-        if (lane == 0) base = atomicAdd(fetch, 32);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n) break;
-        const int k = base + lane;
-        if (k < n) {
-            const int2 e = list[k];
+        int c = 0;
+        if (lane == 0) c = atomicAdd(fetch, 1);
+        c = __shfl_sync(0xffffffffu, c, 0);
+        if (c >= n_chunks) break;
+        int2 e;
+        if (dl.entry(c, lane, n_many, n_single, e)) {
             const int i = e.x;
             HitBest b;
             if (e.y == k_undec_many) {
@@ -434,7 +478,7 @@ __device__ __forceinline__ void resolve_deferred(Job& job, const float4* __restr
                 b = retrace(i, o, d, tmax, exclude);
             } else {
                 b = job.partial(i);
-                redecide<ANY>(tri_in, job.exact(i), e.y, b);
+                redecide<ANY>(tri_in(i), job.exact(i), e.y, b);
             }
             b.undec = k_undec_none;
             job.store(i, trace_result(b));

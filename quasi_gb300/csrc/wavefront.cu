@@ -421,7 +421,11 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
     const int grid_c = sm_count_ * std::max(occ_c, 1);
     const int grid_s = sm_count_ * std::max(occ_s, 1);
     const int grid_shade = sm_count_ * 8;
-    const int grid_fixup = sm_count_ * 4;
+    // The fixup kernels are latency-bound (dependent loads, then double-float arithmetic):
+    // as many blocks as fit.
+    int occ_f = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, k_fixup<ClosestJob>, 128, 0);
+    const int grid_fixup = sm_count_ * std::max(occ_f, 1);
     uint32_t* err = err_dev_.as<uint32_t>();
     unsigned long long* st = stats_dev_.as<unsigned long long>();
     const uint32_t px = width_ * height_;
@@ -446,8 +450,10 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
             int* f_cur = cnt + 2 * D + (k - 1);
             int* f_shadow = cnt + 3 * D + (k - 1);
             const ClosestJob cjob{qcur, hits_.as<float4>(), ray_ff_.as<float4>(), lpath_.as<float4>(),
-                                  DeferList{defer_.as<int2>(), cnt + 4 * D + (k - 1)}, nullptr};
-            const ShadowJob sjob{shadow_.as<float4>(), pd, DeferList{defer_.as<int2>(), cnt + 5 * D + (k - 1)}};
+                                  DeferList{defer_.as<int2>(), cnt + 4 * D + (k - 1), cnt + 8 * D + (k - 1), cap},
+                                  nullptr};
+            const ShadowJob sjob{shadow_.as<float4>(), pd,
+                                 DeferList{defer_.as<int2>(), cnt + 5 * D + (k - 1), cnt + 9 * D + (k - 1), cap}};
             R_TRY(QUASI_LAUNCH(prof_, "trace_closest", s,
                                (kc<<<grid_c, tb, smem_c, s>>>(sd, cjob, c_cur, cap, f_cur, err, st))),
                   "trace_closest");
@@ -714,7 +720,8 @@ int Renderer::stats(Q_cuda_stats* out) {
             st.camera_rays += static_cast<uint64_t>(c[0]);
             for (uint32_t k = 1; k < D; ++k) st.extension_rays += static_cast<uint64_t>(c[k]);
             for (uint32_t k = 0; k < D; ++k) st.shadow_rays += static_cast<uint64_t>(c[D + k]);
-            for (uint32_t k = 0; k < 2 * D; ++k) st.redecided_rays += static_cast<uint64_t>(c[4 * D + k]);
+            for (uint32_t k = 0; k < 2 * D; ++k)
+                st.redecided_rays += static_cast<uint64_t>(c[4 * D + k]) + static_cast<uint64_t>(c[8 * D + k]);
         }
         if (opt_.collect_stats) {
             st.node_visits = stats_host_[0];

@@ -108,9 +108,9 @@ __global__ void __launch_bounds__(256, trace_min_blocks(MODE)) k_trace_shadow(Sc
 // Completes the rays a closest-hit or shadow trace kernel deferred (robust.cuh): re-decides
 // each ray's recorded candidate exactly against its certain result, or re-traces a ray that
 // met more than one (over the 8-wide records when the scene has them: a third of the
-// binary LBVH's dependent node fetches), and stores the final results. The list length is
+// binary LBVH's dependent node fetches), and stores the final results. The list lengths are
 // read on the device, so the launch needs no host synchronisation; a persistent grid takes
-// 32 entries per warp.
+// one chunk of 32 entries per warp (resolve_deferred).
 template <class Job>
 __global__ void __launch_bounds__(128) k_fixup(SceneDev s, Job job, int* __restrict__ fetch,
                                                uint32_t* __restrict__ err) {
@@ -123,15 +123,16 @@ __global__ void __launch_bounds__(128) k_fixup(SceneDev s, Job job, int* __restr
         return trace_bvh<any, false, false, true>(s.nodes, s.tris, s.tri_in, s.n_tris, make_ray(o, d, pad), tmax,
                                                   exclude, e, cnt, job.exact(i));
     };
-    resolve_deferred<any>(job, s.tri_in, job.deferred.list, *job.deferred.count, fetch, retrace);
+    resolve_deferred<any>(job, [&](int) { return s.tri_in; }, job.deferred, fetch, retrace);
     if (e) atomicOr(err, e);
 }
 
 // Per-wave frame counters, k_counters_per_bounce per bounce: [0, D) closest-hit queue
 // lengths, [D, 2D) shadow queue lengths, [2D, 3D) and [3D, 4D) their trace fetch counters,
-// [4D, 5D) and [5D, 6D) the rays each deferred to the fixup kernels, [6D, 8D) the fixup
-// kernels' fetch counters.
-constexpr uint32_t k_counters_per_bounce = 8;
+// [4D, 5D) and [5D, 6D) the rays each deferred with one undecided candidate, [6D, 8D) the
+// fixup kernels' fetch counters, [8D, 9D) and [9D, 10D) the rays each deferred to be
+// re-traced whole.
+constexpr uint32_t k_counters_per_bounce = 10;
 
 // Adds the frame's queue lengths (rays traced) to the cumulative counter stats[4]; one
 // warp, so the timed loop needs no host synchronisation to know how many rays it traced.

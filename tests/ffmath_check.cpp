@@ -3,6 +3,7 @@
 // -ffp-contract=off) reproduces the device results. Prints the worst relative error of each
 // double-float operation against long double over random inputs.
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <random>
 
@@ -12,6 +13,7 @@ inline float __fadd_rn(float a, float b) { return a + b; }
 inline float __fsub_rn(float a, float b) { return a - b; }
 inline float __fmul_rn(float a, float b) { return a * b; }
 inline float __fdiv_rn(float a, float b) { return a / b; }
+inline float __frcp_rn(float a) { return 1.0f / a; }
 inline float __fsqrt_rn(float a) { return std::sqrt(a); }
 inline float __fmaf_rn(float a, float b, float c) { return std::fma(a, b, c); }
 #include "../quasi_gb300/csrc/ffmath.cuh"
