@@ -71,14 +71,16 @@ __global__ void __launch_bounds__(256) k_batch_camera(const BatchSceneDev* __res
                                                       PathDev p, uint2* __restrict__ meta, float4* __restrict__ q,
                                                       int* __restrict__ q_count) {
     const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= paths) return;  // item path counts are multiples of 32: whole warps leave
-    const BatchItem it = items[find_item<false>(items, n_items, gid)];
-    const uint32_t local = item_local(it, gid);
-    meta[gid] = make_uint2(it.scene, local);
     float3 o = mk3(0.f, 0.f, 0.f), d = o;
-    const BatchSceneDev& b = scenes[it.scene];
-    const bool valid = begin_path(b.f, p, gid, local, b.s.nodes, b.s.n_tris, o, d);
-    const int pos = warp_append(0xffffffffu, valid, q_count);
+    bool valid = false;
+    if (gid < paths) {
+        const BatchItem it = items[find_item<false>(items, n_items, gid)];
+        const uint32_t local = item_local(it, gid);
+        meta[gid] = make_uint2(it.scene, local);
+        const BatchSceneDev& b = scenes[it.scene];
+        valid = begin_path(b.f, p, gid, local, b.s.nodes, b.s.n_tris, o, d);
+    }
+    const int pos = block_append(valid, q_count);
     if (valid) {
         q[2 * pos] = make_float4(o.x, o.y, o.z, __int_as_float(static_cast<int>(gid)));
         q[2 * pos + 1] = make_float4(d.x, d.y, d.z, __int_as_float(-1));

@@ -110,4 +110,35 @@ __device__ __forceinline__ int warp_append(uint32_t mask, bool want, int* counte
     return want ? base + __popc(ballot & lanemask_lt()) : -1;
 }
 
+// Reserves queue slots for the threads of a block that want one, with one atomic per block:
+// warp counts by ballot, a scan over the warps in warp 0, one atomicAdd. Every thread of the
+// block calls it (it has two barriers); the block size is a multiple of 32. Returns the
+// thread's slot, or -1 when it wants none. One atomic per block instead of one per warp:
+// every block of a launch appends to the same counter, and same-address atomics are served
+// one at a time by the L2 slice that holds the address.
+__device__ __forceinline__ int block_append(bool want, int* counter) {
+    __shared__ int s_count[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t ballot = __ballot_sync(0xffffffffu, want);
+    if (lane == 0) s_count[warp] = __popc(ballot);
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = static_cast<int>(blockDim.x >> 5);
+        const int c = lane < nw ? s_count[lane] : 0;
+        int incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        int base = 0;
+        if (lane == 0 && total > 0) base = atomicAdd(counter, total);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (lane < nw) s_count[lane] = base + incl - c;
+    }
+    __syncthreads();
+    return want ? s_count[warp] + __popc(ballot & lanemask_lt()) : -1;
+}
+
 }  // namespace quasi

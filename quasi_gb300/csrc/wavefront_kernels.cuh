@@ -45,10 +45,9 @@ __global__ void __launch_bounds__(256) k_pack_tris(const float* __restrict__ raw
 __global__ void __launch_bounds__(256) k_camera(FrameParams f, SceneDev s, PathDev p, float4* __restrict__ q,
                                                 int* __restrict__ q_count) {
     const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= f.wave_spp * f.slots) return;  // slots is a multiple of 32: whole warps leave
     float3 o = mk3(0.f, 0.f, 0.f), d = o;
-    const bool valid = begin_path(f, p, gid, gid, s.nodes, s.n_tris, o, d);
-    const int pos = warp_append(0xffffffffu, valid, q_count);
+    const bool valid = gid < f.wave_spp * f.slots && begin_path(f, p, gid, gid, s.nodes, s.n_tris, o, d);
+    const int pos = block_append(valid, q_count);
     if (valid) {
         q[2 * pos] = make_float4(o.x, o.y, o.z, __int_as_float(static_cast<int>(gid)));
         q[2 * pos + 1] = make_float4(d.x, d.y, d.z, __int_as_float(-1));
@@ -154,10 +153,12 @@ __global__ void __launch_bounds__(256, QUASI_SHADE_MIN_BLOCKS) k_shade(FramePara
                                                int* __restrict__ next_count, float4* __restrict__ shadow_q,
                                                int* __restrict__ shadow_count) {
     const int n = min(*count, capacity);
-    const int lane = threadIdx.x & 31;
     const int stride = gridDim.x * blockDim.x;
-    for (int base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; base < n; base += stride) {
-        const int i = base + lane;
+    // One warp-aggregated atomic per queue and warp: aggregating over the block instead (two
+    // barriers per append) made this kernel 9 % slower; the camera kernel, one short pass per
+    // thread, gained from it (block_append).
+    for (int base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const int i = base + static_cast<int>(threadIdx.x);
         int pid = 0;
         float4 h = make_float4(0.f, __int_as_float(-1), 0.f, 0.f);
         if (i < n) {
