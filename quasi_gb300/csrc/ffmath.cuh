@@ -56,6 +56,16 @@ __device__ __forceinline__ ff ff_add(ff a, ff b) {
 __device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.hi, -a.lo}; }
 __device__ __forceinline__ ff ff_sub(ff a, ff b) { return ff_add(a, ff_neg(b)); }
 
+// a + b with an error below ~2^-47 (|a| + |b|) rather than 2^-47 |a + b| (the QD library's
+// "sloppy" addition: one TwoSum instead of two, 11 operations instead of 20). For operands
+// that already carry rounding of that size (products, rounded positions) the two agree; the
+// exact re-decisions of hit tests keep the accurate form.
+__device__ __forceinline__ ff ff_add_fast(ff a, ff b) {
+    const ff s = two_sum(a.hi, b.hi);
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ ff ff_sub_fast(ff a, ff b) { return ff_add_fast(a, ff_neg(b)); }
+
 __device__ __forceinline__ ff ff_mul(ff a, ff b) {
     ff p = two_prod(a.hi, b.hi);
     p.lo = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, p.lo));
@@ -155,14 +165,14 @@ __device__ __forceinline__ void ff_sincospi(float x, ff& s, ff& c) {
     const ff ps = ff_add(ff{-0.1666666716337204f, 4.967053879312289e-09f},
                          __fmul_rn(f2, __fmaf_rn(f2, -1.984127e-4f, 8.333333e-3f)));
     const ff pc = ff_add(ffv(-0.5f), __fmul_rn(f2, __fmaf_rn(f2, -1.3888889e-3f, 4.1666668e-2f)));
-    const ff sb = ff_add(b, ff_mul(ff_mul(b, b2), ps));
-    const ff cb = ff_add(ffv(1.0f), ff_mul(b2, pc));
+    const ff sb = ff_add_fast(b, ff_mul(ff_mul(b, b2), ps));
+    const ff cb = ff_add_fast(ffv(1.0f), ff_mul(b2, pc));
     const int j = abs(static_cast<int>(jf));
     ff sa{k_sincospi_tab[j][0], k_sincospi_tab[j][1]};
     const ff ca{k_sincospi_tab[j][2], k_sincospi_tab[j][3]};
     if (jf < 0.0f) sa = ff_neg(sa);
-    const ff sv = ff_add(ff_mul(sa, cb), ff_mul(ca, sb));
-    const ff cv = ff_sub(ff_mul(ca, cb), ff_mul(sa, sb));
+    const ff sv = ff_add_fast(ff_mul(sa, cb), ff_mul(ca, sb));
+    const ff cv = ff_sub_fast(ff_mul(ca, cb), ff_mul(sa, sb));
     switch (q) {
         case 0: s = sv; c = cv; break;
         case 1: s = cv; c = ff_neg(sv); break;
@@ -185,6 +195,12 @@ __device__ __forceinline__ ff3 ff3_add(const ff3& a, const ff3& b) {
 __device__ __forceinline__ ff3 ff3_sub(const ff3& a, const ff3& b) {
     return ff3{ff_sub(a.x, b.x), ff_sub(a.y, b.y), ff_sub(a.z, b.z)};
 }
+__device__ __forceinline__ ff3 ff3_add_fast(const ff3& a, const ff3& b) {
+    return ff3{ff_add_fast(a.x, b.x), ff_add_fast(a.y, b.y), ff_add_fast(a.z, b.z)};
+}
+__device__ __forceinline__ ff3 ff3_sub_fast(const ff3& a, const ff3& b) {
+    return ff3{ff_sub_fast(a.x, b.x), ff_sub_fast(a.y, b.y), ff_sub_fast(a.z, b.z)};
+}
 __device__ __forceinline__ ff3 ff3_scale(const ff3& a, ff s) { return ff3{ff_mul(a.x, s), ff_mul(a.y, s), ff_mul(a.z, s)}; }
 __device__ __forceinline__ ff3 ff3_scale(const ff3& a, float s) {
     return ff3{ff_mul(a.x, s), ff_mul(a.y, s), ff_mul(a.z, s)};
@@ -192,6 +208,9 @@ __device__ __forceinline__ ff3 ff3_scale(const ff3& a, float s) {
 __device__ __forceinline__ ff3 ff3_neg(const ff3& a) { return ff3{ff_neg(a.x), ff_neg(a.y), ff_neg(a.z)}; }
 __device__ __forceinline__ ff ff3_dot(const ff3& a, const ff3& b) {
     return ff_add(ff_add(ff_mul(a.x, b.x), ff_mul(a.y, b.y)), ff_mul(a.z, b.z));
+}
+__device__ __forceinline__ ff ff3_dot_fast(const ff3& a, const ff3& b) {
+    return ff_add_fast(ff_add_fast(ff_mul(a.x, b.x), ff_mul(a.y, b.y)), ff_mul(a.z, b.z));
 }
 __device__ __forceinline__ ff3 ff3_cross(const ff3& a, const ff3& b) {
     return ff3{ff_sub(ff_mul(a.y, b.z), ff_mul(a.z, b.y)), ff_sub(ff_mul(a.z, b.x), ff_mul(a.x, b.z)),

@@ -96,10 +96,10 @@ __device__ __forceinline__ void vertex_point(const VertexScene& s, int prim, con
                                              ff3& nrm) {
     const float4 p = __ldg(&s.tri_plane[2 * prim]), q = __ldg(&s.tri_plane[2 * prim + 1]);
     nrm = ff3{ff{p.x, p.y}, ff{p.z, p.w}, ff{q.x, q.y}};
-    const ff den = ff3_dot(nrm, rd);
+    const ff den = ff3_dot_fast(nrm, rd);
     if (den.hi != 0.0f) {
-        const ff t = ff_div(ff_sub(ff{q.z, q.w}, ff3_dot(nrm, ro)), den);
-        x = ff3_add(ro, ff3_scale(rd, t));
+        const ff t = ff_div(ff_sub_fast(ff{q.z, q.w}, ff3_dot_fast(nrm, ro)), den);
+        x = ff3_add_fast(ro, ff3_scale(rd, t));
     } else {
         // A ray parallel to the plane cannot hit the triangle (an exact hit needs
         // det = -d.(e1 x e2) != 0); kept only so that x is defined.
@@ -110,7 +110,7 @@ __device__ __forceinline__ void vertex_point(const VertexScene& s, int prim, con
 
 // Continuation origin x + eps n.
 __device__ __forceinline__ ff3 vertex_origin(const VertexScene& s, const ff3& x, const ff3& nrm) {
-    return ff3_add(x, ff3_scale(nrm, s.eps));
+    return ff3_add_fast(x, ff3_scale(nrm, s.eps));
 }
 
 // Cosine-weighted continuation direction about n = nrm (plugin.mm:111-125) in double-float:
@@ -131,17 +131,17 @@ __device__ __forceinline__ ff3 vertex_dir(const ff3& nrm, float r3, float r4) {
     ff3 c, nc;  // c = cross(n, a), nc = cross(n, c)
     ff cc;      // |c|^2
     if (fabsf(x.hi) > 0.9f) {
-        cc = ff_add(ff_mul(x, x), ff_mul(z, z));
+        cc = ff_add_fast(ff_mul(x, x), ff_mul(z, z));
         c = ff3{ff_neg(z), ffv(0.0f), x};
         nc = ff3{ff_mul(x, y), ff_neg(cc), ff_mul(y, z)};
     } else {
-        cc = ff_add(ff_mul(y, y), ff_mul(z, z));
+        cc = ff_add_fast(ff_mul(y, y), ff_mul(z, z));
         c = ff3{ffv(0.0f), z, ff_neg(y)};
         nc = ff3{ff_neg(cc), ff_mul(x, y), ff_mul(x, z)};
     }
     const ff g = ff_div(sin_t, ff_sqrt(cc));
     const ff wu = ff_mul(cphi, g), wv = ff_mul(sphi, g);
-    return ff3_add(ff3_add(ff3_scale(nc, wu), ff3_scale(c, wv)), ff3_scale(nrm, cos_t));
+    return ff3_add_fast(ff3_add_fast(ff3_scale(nc, wu), ff3_scale(c, wv)), ff3_scale(nrm, cos_t));
 }
 
 // The NEE sample of a vertex at x (normal nrm, continuation origin org) towards the light
@@ -156,14 +156,14 @@ __device__ __forceinline__ void vertex_light(const VertexScene& s, int prim, con
     const ff3 le1 = ff3_diff(xyz(lt.v1), la);
     const ff3 le2 = ff3_diff(xyz(lt.v2), la);
     const ff su = ff_sqrt(ffv(r1));
-    const ff3 yl = ff3_add(ff3_add(ff3v(la), ff3_scale(le1, ff_mul(su, two_sum(1.0f, -r2)))),
-                           ff3_scale(le2, ff_mul(su, r2)));
+    const ff3 yl = ff3_add_fast(ff3_add_fast(ff3v(la), ff3_scale(le1, ff_mul(su, two_sum(1.0f, -r2)))),
+                                ff3_scale(le2, ff_mul(su, r2)));
     // (y - x) first, in double-float: both lie on their planes, so a small surface-to-light
     // gap keeps its digits; subtracting the rounded offset origin would not. The light sample
     // only weights this vertex (nothing of it carries to the next bounce), so once that
     // difference is formed the eps offset, length, direction and cosines are FP32: relative
     // errors ~1e-7 against the 1e-4 bound.
-    const float3 d0 = ff3_f(ff3_sub(yl, x));
+    const float3 d0 = ff3_f(ff3_sub_fast(yl, x));
     const float3 nf = ff3_f(nrm);
     const float3 dv = mk3(__fsub_rn(d0.x, __fmul_rn(s.eps, nf.x)), __fsub_rn(d0.y, __fmul_rn(s.eps, nf.y)),
                           __fsub_rn(d0.z, __fmul_rn(s.eps, nf.z)));
@@ -181,9 +181,9 @@ __device__ __forceinline__ void vertex_light(const VertexScene& s, int prim, con
         // normal towards the shading side, to just short of the lifted shading point:
         // neither end's plane (nor a coplanar neighbour) can be crossed.
         const float side = cl < 0.0f ? s.eps : -s.eps;
-        const ff3 so = ff3_add(yl, ff3_scale(nl, side));
+        const ff3 so = ff3_add_fast(yl, ff3_scale(nl, side));
         out.seg_o = so;
-        out.seg_d = ff3_sub(org, so);
+        out.seg_d = ff3_sub_fast(org, so);
         const float3 sd = ff3_f(out.seg_d);
         const float sdist = __fsqrt_rn(fdot3(sd, sd));
         const float inv_s = __fdiv_rn(1.0f, sdist);

@@ -24,7 +24,7 @@ static long double val(ff a) { return (long double)a.hi + (long double)a.lo; }
 int main() {
     std::mt19937_64 rng(7);
     std::uniform_real_distribution<double> U(-2.0, 2.0), P(1e-3, 4.0), R01(0.0, 1.0);
-    long double e_add = 0, e_mul = 0, e_div = 0, e_sqrt = 0, e_sin = 0, e_cos = 0;
+    long double e_add = 0, e_addf = 0, e_mul = 0, e_div = 0, e_sqrt = 0, e_sin = 0, e_cos = 0;
     auto mk = [&](double d) { ff x; x.hi = (float)d; x.lo = (float)(d - (double)x.hi); return x; };
     for (int i = 0; i < 200000; ++i) {
         const ff a = mk(U(rng)), b = mk(U(rng)), p = mk(P(rng));
@@ -34,6 +34,7 @@ int main() {
         };
         const long double scale = fmaxl(fabsl(A), fabsl(B));
         e_add = fmaxl(e_add, fabsl(val(quasi::ff_add(a, b)) - (A + B)) / fmaxl(scale, 1e-30L));
+        e_addf = fmaxl(e_addf, fabsl(val(quasi::ff_add_fast(a, b)) - (A + B)) / fmaxl(fabsl(A) + fabsl(B), 1e-30L));
         e_mul = fmaxl(e_mul, rel(val(quasi::ff_mul(a, b)), A * B));
         e_div = fmaxl(e_div, rel(val(quasi::ff_div(a, p)), A / Pv));
         e_sqrt = fmaxl(e_sqrt, rel(val(quasi::ff_sqrt(p)), sqrtl(Pv)));
@@ -44,7 +45,7 @@ int main() {
         e_sin = fmaxl(e_sin, fabsl(val(s) - sinl(pi * (long double)x)));
         e_cos = fmaxl(e_cos, fabsl(val(c) - cosl(pi * (long double)x)));
     }
-    std::printf("add %.3Le\nmul %.3Le\ndiv %.3Le\nsqrt %.3Le\nsin %.3Le\ncos %.3Le\n", e_add, e_mul, e_div, e_sqrt,
-                e_sin, e_cos);
+    std::printf("add %.3Le\naddf %.3Le\nmul %.3Le\ndiv %.3Le\nsqrt %.3Le\nsin %.3Le\ncos %.3Le\n", e_add, e_addf,
+                e_mul, e_div, e_sqrt, e_sin, e_cos);
     return 0;
 }
