@@ -186,7 +186,7 @@ typedef struct Q_cuda_options {
     uint32_t seed;               /* RNG seed (0) */
     uint32_t integrator;         /* QUASI_INTEGRATOR_* */
     uint32_t rebuild_each_frame; /* rebuild the LBVH in every frame (1 = yes) */
-    uint32_t wave_spp;           /* samples per pixel per wavefront (0 = as many as fit ~64M
+    uint32_t wave_spp;           /* samples per pixel per wavefront (0 = as many as fit 2^27
                                     path slots, fewer if free device memory is short) */
     uint32_t trace_block;        /* threads per block of the trace kernels (0 = 256 over the 8-wide records, 128 binary) */
     uint32_t record_samples;     /* keep per-sample radiance and path signatures */
@@ -366,7 +366,8 @@ typedef struct Q_cuda_batch_options {
     uint32_t max_depth;     /* path vertices after the camera (6) */
     uint32_t seed;          /* RNG seed, shared by all scenes (0) */
     uint32_t form;          /* QUASI_BATCH_WAVEFRONT (default) or QUASI_BATCH_MEGAKERNEL */
-    uint32_t wave_paths;    /* path slots per wave (0 = 64M; raised to the largest sample plane) */
+    uint32_t wave_paths;    /* path slots per wave (0 = 2^27, fewer if device memory is short; at most 2^27;
+                               raised to the largest sample plane) */
     uint32_t trace_block;   /* threads per block of the persistent kernels (0 = 128) */
     uint32_t fetch_rays;    /* rays or paths a warp takes per atomic, multiple of 32 (0 = 32) */
     uint32_t use_graph;     /* 0 = default (graph), 1 = graph, 2 = plain launches */

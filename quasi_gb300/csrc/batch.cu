@@ -22,8 +22,8 @@ CameraFF make_camera_basis(const Q_camera& c, uint32_t w, uint32_t h);  // wavef
 namespace {
 
 inline uint32_t ceil_div(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
-constexpr uint32_t k_default_wave_paths = 64u << 20;  // as the single-scene renderer's waves
-constexpr uint32_t k_max_wave_paths = 1u << 26;
+constexpr uint32_t k_default_wave_paths = 1u << 27;  // as the single-scene renderer's waves
+constexpr uint32_t k_max_wave_paths = 1u << 27;
 
 }  // namespace
 
@@ -729,7 +729,7 @@ int BatchRenderer::autotune(double budget_ms, Q_cuda_batch_options* chosen) {
         if (rc) return rc;
     }
     const uint32_t forms[] = {QUASI_BATCH_WAVEFRONT, QUASI_BATCH_MEGAKERNEL};
-    const uint32_t waves[] = {8u << 20, 16u << 20, 32u << 20, 64u << 20};
+    const uint32_t waves[] = {16u << 20, 32u << 20, 64u << 20, 128u << 20};
     const uint32_t blocks[] = {64, 128, 256};
     const uint32_t fetches[] = {32, 64, 128};
     const uint32_t refills[] = {4, 8, 16};

@@ -274,11 +274,12 @@ uint32_t Renderer::effective_wave_spp(uint32_t spp) const {
     if (opt_.wave_spp > 0) return std::min(opt_.wave_spp, spp);
     const uint32_t tiles = ceil_div(width_, 8) * ceil_div(height_, 4);
     const uint32_t slots = tiles * 32;
-    // ~64M paths per wave (~16 GB of wave state): the later bounces of a wave shrink as paths
-    // end, and larger waves keep those queues long enough to fill the GPU (1080p, 64 spp on
-    // the 1M soup: 2 spp per wave 885, 4 spp 971, 8 spp 1024, 16 spp 1053, 32 spp 1071,
-    // 64 spp 1080 Mrays/s on GB300)
-    const uint64_t target = wave_paths_fitting(64u << 20, k_wave_bytes_per_path,
+    // up to 2^27 paths per wave (~36 GB of wave state, all 64 samples of a 1080p frame): the
+    // later bounces of a wave shrink as paths end, larger waves keep those queues long enough
+    // to fill the GPU, and every wave pays each kernel's fixed drain once (1080p, 64 spp on
+    // the 1M soup, GB300: 16 spp per wave 1403.5, 32 spp 1441.8, 64 spp 1462.9 Mrays/s; the
+    // fixup kernels, whose time is mostly a fixed tail per launch, halve with the waves)
+    const uint64_t target = wave_paths_fitting(1u << 27, k_wave_bytes_per_path,
                                                size_t(wave_capacity_) * k_wave_bytes_per_path);
     return std::max<uint32_t>(1, static_cast<uint32_t>(std::min<uint64_t>(spp, target / std::max<uint32_t>(slots, 1))));
 }
