@@ -129,6 +129,7 @@ private:
     DeviceBuffer aov_normal_;     // float4 per pixel: sum of remapped normal
     DeviceBuffer record_rad_;     // per-sample radiance (record_samples)
     DeviceBuffer record_sig_;     // per-sample signatures (record_samples)
+    DeviceBuffer resolve_;        // float4 per pixel: the image a readback copies to the host
     uint32_t record_spp_ = 0;
 
     // wavefront

@@ -73,7 +73,8 @@ Renderer::~Renderer() {
     if (stream_) cudaStreamSynchronize(stream_);
     bvh_.release();
     for (DeviceBuffer* b : {&raw_vertices_, &tri_in_, &albedo_, &emission_, &emitters_, &quads_, &accum_, &comp_,
-                            &aov_albedo_, &aov_normal_, &record_rad_, &record_sig_, &queue_[0], &queue_[1], &hits_,
+                            &aov_albedo_, &aov_normal_, &record_rad_, &record_sig_, &resolve_, &queue_[0], &queue_[1],
+                            &hits_,
                             &shadow_, &beta_, &lpath_, &aov_a_, &aov_n_, &sig_, &ray_ff_, &defer_,
                             &counters_, &stats_dev_, &err_dev_})
         b->release();
@@ -646,24 +647,20 @@ int Renderer::resolve_device(float* device_rgba) {
 int Renderer::resolve_host(float* beauty, float* albedo, float* normal, float* depth) {
     if (!accum_.ptr) return fail(QUASI_ERR_STATE, "nothing rendered");
     const uint32_t px = width_ * height_;
-    DeviceBuffer tmp;
-    R_TRY(tmp.reserve(sizeof(float4) * px), "resolve buffer");
+    // kept between readbacks: a cudaFree per call would synchronise the device
+    R_TRY(resolve_.reserve(sizeof(float4) * px), "resolve buffer");
     float* outs[4] = {beauty, albedo, normal, depth};
     for (int mode = 0; mode < 4; ++mode) {
         if (!outs[mode]) continue;
         cudaError_t e = QUASI_LAUNCH(prof_, "resolve", stream_,
                                      (k_resolve<<<ceil_div(px, 256), 256, 0, stream_>>>(
                                          accum_.as<float4>(), aov_albedo_.as<float4>(), aov_normal_.as<float4>(), px,
-                                         float(samples_), mode, tmp.as<float4>())));
+                                         float(samples_), mode, resolve_.as<float4>())));
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(outs[mode], tmp.ptr, sizeof(float4) * px, cudaMemcpyDeviceToHost, stream_);
+            e = cudaMemcpyAsync(outs[mode], resolve_.ptr, sizeof(float4) * px, cudaMemcpyDeviceToHost, stream_);
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
-        if (e != cudaSuccess) {
-            tmp.release();
-            return cuda_fail(e, "resolve");
-        }
+        if (e != cudaSuccess) return cuda_fail(e, "resolve");
     }
-    tmp.release();
     return QUASI_OK;
 }
 

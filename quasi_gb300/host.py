@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 from contextlib import contextmanager
 from dataclasses import dataclass, field
 from pathlib import Path
@@ -219,13 +220,18 @@ class PluginHost:
                 raise QuasiError("Q_plugin_render", A.QUASI_ERR_CUDA, msg)
 
     def readback(self) -> np.ndarray:
+        """The mean beauty image as an (H, W, 4) float32 array over the plugin's own buffer
+        (no copy): Q_plugin_readback_free runs when the array is garbage-collected."""
         r = self.lib.Q_plugin_readback(self.handle)
         if not r.data:
             raise QuasiError("Q_plugin_readback", A.QUASI_ERR_STATE, "no data")
         try:
-            return np.ctypeslib.as_array(r.data, shape=(r.height, r.width, r.channels)).copy()
-        finally:
+            arr = np.ctypeslib.as_array(r.data, shape=(r.height, r.width, r.channels))
+        except BaseException:
             self.lib.Q_plugin_readback_free(C.byref(r))
+            raise
+        weakref.finalize(arr, self.lib.Q_plugin_readback_free, C.byref(r))
+        return arr
 
     def readback_aov(self) -> dict[str, np.ndarray]:
         r = self.lib.Q_plugin_readback_aov(self.handle)
