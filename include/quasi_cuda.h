@@ -203,6 +203,9 @@ typedef struct Q_cuda_options {
                                     between refill checks (0 = default) */
     uint32_t bvh_width;          /* traversal structure: 8 = 8-wide records collapsed from the
                                     LBVH (default, 0), 2 = the binary LBVH nodes */
+    uint32_t bvh_cluster;        /* the LBVH's largest subtrees of at most this many leaves are
+                                    rebuilt with the least surface-area split (0 = default 32;
+                                    3..32; 1 or 2 = none: the plain Morton hierarchy) */
 } Q_cuda_options;
 
 /* Counters of the last frame (rays actually traced) and of the whole accumulation. */

@@ -372,6 +372,239 @@ __device__ __forceinline__ uint32_t wide_exponent(float lo, float hi) {
     return static_cast<uint32_t>(e + 127);
 }
 
+// ---------------------------------------------------------------- SAH refinement of small subtrees
+//
+// The Morton order places a subtree's leaves well at large scale but splits small groups of
+// triangles by their code bits, not by their boxes. Each maximal subtree of 3..cluster leaves
+// (cluster <= 32: one warp lane per leaf) is rebuilt top-down with the split of least
+// surface-area cost (areas of the two child boxes times their leaf counts) over every
+// position of the leaves sorted along each axis by box centre; the subtree keeps its root
+// node, its set of node indices and its leaves, so the rest of the tree is untouched. On the
+// 1M soup this cuts the 8-wide records a ray visits by 2-3 % (a full top-down SAH build:
+// 5 %).
+
+// Roots of the maximal subtrees with 3..cluster leaves (their parent covers more).
+__global__ void __launch_bounds__(256) k_sah_roots(const float4* __restrict__ nodes, const int* __restrict__ parent,
+                                                   int n, int cluster, int* __restrict__ roots,
+                                                   int* __restrict__ count) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n - 1) return;
+    const float4 m = __ldg(&nodes[4 * c + 3]);
+    const int size = __float_as_int(m.w) - __float_as_int(m.z) + 1;
+    if (size < 3 || size > cluster) return;
+    if (c != 0) {
+        const float4 pm = __ldg(&nodes[4 * __ldg(&parent[c]) + 3]);
+        if (__float_as_int(pm.w) - __float_as_int(pm.z) + 1 <= cluster) return;
+    }
+    roots[atomicAdd(count, 1)] = c;
+}
+
+// Inclusive scan over the warp's lanes of a box (min of lo, max of hi) and a count; reverse
+// = true scans from lane 31 down.
+template <bool REVERSE>
+__device__ __forceinline__ void warp_box_scan(float (&lo)[3], float (&hi)[3], int& cnt, int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        float l[3], h[3];
+        int c;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            l[a] = REVERSE ? __shfl_down_sync(0xffffffffu, lo[a], o) : __shfl_up_sync(0xffffffffu, lo[a], o);
+            h[a] = REVERSE ? __shfl_down_sync(0xffffffffu, hi[a], o) : __shfl_up_sync(0xffffffffu, hi[a], o);
+        }
+        c = REVERSE ? __shfl_down_sync(0xffffffffu, cnt, o) : __shfl_up_sync(0xffffffffu, cnt, o);
+        if (REVERSE ? lane + o < 32 : lane >= o) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = fminf(lo[a], l[a]);
+                hi[a] = fmaxf(hi[a], h[a]);
+            }
+            cnt += c;
+        }
+    }
+}
+
+// One warp per subtree root from k_sah_roots.
+__global__ void __launch_bounds__(256) k_sah_rebuild(const float4* __restrict__ tri_in,
+                                                     const uint32_t* __restrict__ order, float4* nodes,
+                                                     const int* __restrict__ roots, const int* __restrict__ count,
+                                                     uint32_t* __restrict__ err) {
+    constexpr int W = 8;  // warps per block
+    __shared__ int s_pool[W][32];       // the subtree's node indices, root first
+    __shared__ uint2 s_task[W][32];     // pending (leaf mask, node index)
+    __shared__ float s_box[W][3][32][6];  // leaf boxes in centre order along each axis
+    __shared__ int s_lane[W][3][32];    // lane (leaf) at each rank along each axis
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n_roots = *count;
+    for (int ci = blockIdx.x * W + warp; ci < n_roots; ci += gridDim.x * W) {
+        const int r0 = roots[ci];
+        const float4 m3 = nodes[4 * r0 + 3];
+        const int f = __float_as_int(m3.z), m = __float_as_int(m3.w) - f + 1;  // 3..32 leaves
+        int np = 0;
+        if (lane == 0) {  // the subtree's internal nodes, depth first (m - 1 of them)
+            int st[32], sp = 0;
+            st[sp++] = r0;
+            while (sp > 0 && np < 32) {
+                const int c = st[--sp];
+                s_pool[warp][np++] = c;
+                const float4 q = nodes[4 * c + 3];
+                const int a = __float_as_int(q.x), b = __float_as_int(q.y);
+                if (a >= 0 && sp < 32) st[sp++] = a;
+                if (b >= 0 && sp < 32) st[sp++] = b;
+            }
+        }
+        np = __shfl_sync(0xffffffffu, np, 0);
+        if (np != m - 1) {  // not the subtree the leaf range says: leave it as it is
+            if (lane == 0) atomicOr(err, k_deverr_traversal);
+            continue;
+        }
+        // this lane's leaf: box and centre
+        const bool have = lane < m;
+        float lo[3], hi[3], ce[3];
+        if (have) {
+            const uint32_t o = order[f + lane];
+            const float4 a = __ldg(&tri_in[3 * o]), b = __ldg(&tri_in[3 * o + 1]), c = __ldg(&tri_in[3 * o + 2]);
+            lo[0] = fminf(a.x, fminf(b.x, c.x));
+            lo[1] = fminf(a.y, fminf(b.y, c.y));
+            lo[2] = fminf(a.z, fminf(b.z, c.z));
+            hi[0] = fmaxf(a.x, fmaxf(b.x, c.x));
+            hi[1] = fmaxf(a.y, fmaxf(b.y, c.y));
+            hi[2] = fmaxf(a.z, fmaxf(b.z, c.z));
+#pragma unroll
+            for (int k = 0; k < 3; ++k) ce[k] = __fadd_rn(lo[k], hi[k]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = __int_as_float(0x7f800000);
+                hi[k] = -__int_as_float(0x7f800000);
+                ce[k] = __int_as_float(0x7f800000);
+            }
+        }
+        // rank of this leaf along each axis (centre, then lane), and the boxes in rank order
+        int rank[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            int r = 0;
+            for (int j = 0; j < 32; ++j) {
+                const float cj = __shfl_sync(0xffffffffu, ce[k], j);
+                r += (cj < ce[k] || (cj == ce[k] && j < lane)) ? 1 : 0;
+            }
+            rank[k] = r;
+            s_box[warp][k][r][0] = lo[0];
+            s_box[warp][k][r][1] = lo[1];
+            s_box[warp][k][r][2] = lo[2];
+            s_box[warp][k][r][3] = hi[0];
+            s_box[warp][k][r][4] = hi[1];
+            s_box[warp][k][r][5] = hi[2];
+            s_lane[warp][k][r] = lane;
+        }
+        if (lane == 0) s_task[warp][0] = make_uint2(m == 32 ? 0xffffffffu : (1u << m) - 1u, static_cast<uint32_t>(r0));
+        __syncwarp();
+        int n_task = 1, n_used = 1;  // warp-uniform: pending tasks, pool entries handed out
+        for (int it = 0; n_task > 0; ++it) {
+            if (it >= 64) {
+                if (lane == 0) atomicOr(err, k_deverr_traversal);
+                break;
+            }
+            const uint2 task = s_task[warp][--n_task];
+            const uint32_t mask = task.x;
+            // best split over the three axes: leaves of rank <= r go left
+            float best = __int_as_float(0x7f800000);
+            int best_axis = 0, best_r = 0;
+            float bl[6], br[6];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const bool member = (mask >> s_lane[warp][k][lane]) & 1u;
+                float pl[3], ph[3], sl[3], sh[3];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    pl[a] = member ? s_box[warp][k][lane][a] : __int_as_float(0x7f800000);
+                    ph[a] = member ? s_box[warp][k][lane][3 + a] : -__int_as_float(0x7f800000);
+                    sl[a] = pl[a];
+                    sh[a] = ph[a];
+                }
+                int pc = member ? 1 : 0, sc = pc;
+                warp_box_scan<false>(pl, ph, pc, lane);
+                warp_box_scan<true>(sl, sh, sc, lane);
+                // split after rank `lane`: left = prefix(lane), right = suffix(lane + 1)
+                float rl[3], rh[3];
+                int rc = __shfl_down_sync(0xffffffffu, sc, 1);
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    rl[a] = __shfl_down_sync(0xffffffffu, sl[a], 1);
+                    rh[a] = __shfl_down_sync(0xffffffffu, sh[a], 1);
+                }
+                if (lane == 31) rc = 0;
+                float cost = __int_as_float(0x7f800000);
+                if (member && pc > 0 && rc > 0) {
+                    const float al = half_area(pl, ph), ar = half_area(rl, rh);
+                    cost = __fadd_rn(__fmul_rn(al, static_cast<float>(pc)), __fmul_rn(ar, static_cast<float>(rc)));
+                }
+                // warp argmin (cost, rank)
+                float c = cost;
+                int r = lane;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const float c2 = __shfl_xor_sync(0xffffffffu, c, o);
+                    const int r2 = __shfl_xor_sync(0xffffffffu, r, o);
+                    if (c2 < c || (c2 == c && r2 < r)) {
+                        c = c2;
+                        r = r2;
+                    }
+                }
+                if (c < best) {
+                    best = c;
+                    best_axis = k;
+                    best_r = r;
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        bl[a] = __shfl_sync(0xffffffffu, pl[a], r);
+                        bl[3 + a] = __shfl_sync(0xffffffffu, ph[a], r);
+                        br[a] = __shfl_sync(0xffffffffu, rl[a], r);
+                        br[3 + a] = __shfl_sync(0xffffffffu, rh[a], r);
+                    }
+                }
+            }
+            if (!(best < __int_as_float(0x7f800000))) {  // no split found: keep the old tree shape
+                if (lane == 0) atomicOr(err, k_deverr_traversal);
+                break;
+            }
+            const bool mine = (mask >> lane) & 1u;
+            const uint32_t left = __ballot_sync(0xffffffffu, mine && rank[best_axis] <= best_r);
+            const uint32_t right = mask & ~left;
+            const uint32_t side[2] = {left, right};
+            const int need = (__popc(left) > 1 ? 1 : 0) + (__popc(right) > 1 ? 1 : 0);
+            if (left == 0u || right == 0u || n_used + need > m - 1 || n_task + need > 32) {
+                if (lane == 0) atomicOr(err, k_deverr_traversal);
+                break;
+            }
+            int ref[2];
+#pragma unroll
+            for (int s2 = 0; s2 < 2; ++s2) {
+                if (__popc(side[s2]) == 1) {
+                    ref[s2] = ~(f + __ffs(side[s2]) - 1);
+                } else {
+                    ref[s2] = s_pool[warp][n_used];
+                    if (lane == 0) s_task[warp][n_task] = make_uint2(side[s2], static_cast<uint32_t>(ref[s2]));
+                    ++n_used;
+                    ++n_task;
+                }
+            }
+            if (lane == 0) {
+                float4* nd = nodes + 4 * static_cast<size_t>(task.y);
+                nd[0] = make_float4(bl[0], bl[3], bl[1], bl[4]);
+                nd[1] = make_float4(br[0], br[3], br[1], br[4]);
+                nd[2] = make_float4(bl[2], bl[5], br[2], br[5]);
+                // (z, w): a leaf range of the node's leaf count (the collapse reads only the count)
+                nd[3] = make_float4(__int_as_float(ref[0]), __int_as_float(ref[1]), __int_as_float(f),
+                                    __int_as_float(f + __popc(mask) - 1));
+            }
+            __syncwarp();
+        }
+        __syncwarp();
+    }
+}
+
 // One thread per binary internal node b: the wide record of b's subtree (layout in wide.cuh).
 __global__ void __launch_bounds__(128) k_collapse8(const float4* __restrict__ nodes, int n_internal,
                                                    float4* __restrict__ wide) {
@@ -643,6 +876,8 @@ cudaError_t LbvhBuilder::reserve(uint32_t n) {
     QUASI_TRY_CUDA(cudaMalloc(&tris_, sizeof(float4) * 3 * m));
     QUASI_TRY_CUDA(cudaMalloc(&wide_, sizeof(float4) * k_wide_node_f4 * m));
     QUASI_TRY_CUDA(cudaMalloc(&tri_plane_, sizeof(float4) * 2 * m));
+    QUASI_TRY_CUDA(cudaMalloc(&sah_roots_, sizeof(int) * m));
+    QUASI_TRY_CUDA(cudaMalloc(&sah_count_, sizeof(int)));
     QUASI_TRY_CUDA(radix_sort_reserve(sort_, m));
     capacity_ = m;
     return cudaSuccess;
@@ -652,12 +887,14 @@ void LbvhBuilder::release() {
     for (void* p : {static_cast<void*>(bounds_), static_cast<void*>(partial_), static_cast<void*>(morton_),
                     static_cast<void*>(keys_), static_cast<void*>(order_), static_cast<void*>(parent_),
                     static_cast<void*>(flags_), static_cast<void*>(nodes_), static_cast<void*>(tris_),
-                    static_cast<void*>(wide_), static_cast<void*>(tri_plane_), static_cast<void*>(emit_tab_)})
+                    static_cast<void*>(wide_), static_cast<void*>(tri_plane_), static_cast<void*>(emit_tab_),
+                    static_cast<void*>(sah_roots_), static_cast<void*>(sah_count_)})
         if (p) cudaFree(p);
     bounds_ = partial_ = nullptr;
     morton_ = keys_ = order_ = flags_ = nullptr;
     parent_ = nullptr;
     nodes_ = tris_ = wide_ = tri_plane_ = emit_tab_ = nullptr;
+    sah_roots_ = sah_count_ = nullptr;
     emit_capacity_ = 0;
     if (tree_) cudaFree(tree_);
     tree_ = nullptr;
@@ -704,6 +941,17 @@ cudaError_t LbvhBuilder::build(const float4* tri_in, uint32_t n, const int* emit
     QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_leaf_boxes", stream,
                                 (k_leaf_boxes<<<ceil_div(n, 256), 256, 0, stream>>>(
                                     tri_in, order_, static_cast<int>(n), parent_, nodes_, flags_, tris_, err))));
+    if (sah_cluster_ >= 3 && n >= 3) {
+        QUASI_TRY_CUDA(cudaMemsetAsync(sah_count_, 0, sizeof(int), stream));
+        QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_sah_roots", stream,
+                                    (k_sah_roots<<<ceil_div(n - 1, 256), 256, 0, stream>>>(
+                                        nodes_, parent_, static_cast<int>(n), sah_cluster_, sah_roots_, sah_count_))));
+        // at most one root per 3 leaves; 8 per block, a block per 24 leaves up to a full GPU
+        const uint32_t blocks = std::max<uint32_t>(1, std::min<uint32_t>(ceil_div(n, 24), 152u * 8u));
+        QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_sah_rebuild", stream,
+                                    (k_sah_rebuild<<<blocks, 256, 0, stream>>>(tri_in, order_, nodes_, sah_roots_,
+                                                                               sah_count_, err))));
+    }
     const uint32_t internal = n > 1 ? n - 1 : 1;
     QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_collapse8", stream,
                                 (k_collapse8<<<ceil_div(internal, 128), 128, 0, stream>>>(

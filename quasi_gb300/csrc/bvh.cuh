@@ -74,6 +74,10 @@ public:
     cudaError_t build(const float4* tri_in, uint32_t n, const int* emitters, uint32_t n_emit, cudaStream_t stream,
                       KernelProfiler& prof, uint32_t* err);
 
+    // Leaves of the largest subtrees rebuilt with the surface-area split after the Morton
+    // hierarchy (3..32; below 3: the plain LBVH).
+    void set_sah_cluster(int leaves) { sah_cluster_ = leaves < 3 ? 0 : (leaves > 32 ? 32 : leaves); }
+
     // Copies the top max_nodes internal nodes (breadth first) for staging in shared memory.
     cudaError_t build_treelet(int max_nodes, cudaStream_t stream, KernelProfiler& prof);
 
@@ -104,6 +108,9 @@ private:
     float4* tri_plane_ = nullptr;    // 32 bytes per triangle (shading normal and plane offset)
     float4* emit_tab_ = nullptr;     // 80 bytes per emitter (light-sampling records)
     uint32_t emit_capacity_ = 0;
+    int sah_cluster_ = 32;           // leaves of the subtrees rebuilt with the SAH split (0: none)
+    int* sah_roots_ = nullptr;       // roots of those subtrees
+    int* sah_count_ = nullptr;
     float4* tree_ = nullptr;
     int tree_n_ = 0;
     int tree_capacity_ = 0;

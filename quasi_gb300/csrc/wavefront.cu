@@ -216,8 +216,14 @@ int Renderer::set_options(const Q_cuda_options& o) {
         return fail(QUASI_ERR_INVALID, "smem_levels must be 0 (default), 1..9, or 32 (none)");
     if (n.bvh_width != 0 && n.bvh_width != 2 && n.bvh_width != 8)
         return fail(QUASI_ERR_INVALID, "bvh_width must be 0 (default), 2 or 8");
+    if (n.bvh_cluster > 32) return fail(QUASI_ERR_INVALID, "bvh_cluster must be at most 32");
+    if (n.bvh_cluster == 0) n.bvh_cluster = 32;
     const bool changed = n.seed != opt_.seed || n.max_depth != opt_.max_depth || n.integrator != opt_.integrator ||
                          n.ray_eps != opt_.ray_eps;
+    if (n.bvh_cluster != opt_.bvh_cluster) {
+        bvh_.set_sah_cluster(static_cast<int>(n.bvh_cluster));
+        bvh_dirty_ = true;
+    }
     opt_ = n;
     prof_.set_enabled(opt_.profile != 0);
     if (changed) return reset();

@@ -15,6 +15,7 @@ pytestmark = pytest.mark.gpu
 @pytest.fixture(scope="module")
 def host(cuda_ok):
     h = q.PluginHost(width=32, height=32)
+    h.set_options(bvh_cluster=1)  # the plain Morton hierarchy (no surface-area refinement)
     yield h
     h.destroy()
 

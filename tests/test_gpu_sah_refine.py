@@ -1,0 +1,131 @@
+"""Surface-area refinement of the LBVH (bvh_cluster): the largest subtrees of at most 32
+leaves are rebuilt with the least-cost split. Checked as a hierarchy (every leaf once, every
+child box the exact union of its triangles' boxes, the 8-wide records covering and
+containing what they hold), as an improvement (lower surface-area sum, fewer record
+visits), and by its effect on images: none, since every hit decision is exact, so frames
+rendered over the refined and the plain hierarchy are identical bit for bit."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import quasi_gb300 as q
+from test_wide_oracle import _decode
+
+pytestmark = pytest.mark.gpu
+
+
+def _tri_boxes(vertices: np.ndarray, order: np.ndarray):
+    v = vertices.reshape(-1, 3, 3)[order]
+    return v.min(axis=1), v.max(axis=1)
+
+
+def _leaf_sets(children: np.ndarray, n: int) -> list[np.ndarray]:
+    """Leaf positions under each internal node (children: 2 per node, ~pos for a leaf)."""
+    sets: list[np.ndarray | None] = [None] * max(n - 1, 1)
+    order, todo = [], [0]
+    while todo:  # pre-order, then children before parents when reversed
+        c = todo.pop()
+        order.append(c)
+        for k in (0, 1):
+            ch = int(children[2 * c + k])
+            if ch >= 0:
+                todo.append(ch)
+    for c in reversed(order):
+        parts = []
+        for k in (0, 1):
+            ch = int(children[2 * c + k])
+            parts.append(np.array([~ch]) if ch < 0 else sets[ch])
+        sets[c] = np.concatenate(parts)
+    return sets
+
+
+def _area_sum(boxes: np.ndarray) -> float:
+    b = boxes.reshape(-1, 2, 2, 3).astype(np.float64)  # node, child, lo/hi, axis
+    d = b[:, :, 1] - b[:, :, 0]
+    return float((d[..., 0] * d[..., 1] + d[..., 1] * d[..., 2] + d[..., 2] * d[..., 0]).sum())
+
+
+@pytest.mark.parametrize("spec", ["cornell36", "soup:n=1000,seed=3", "soup:n=65537,seed=11"])
+def test_refined_hierarchy_is_valid_and_better(cuda_ok, orc, spec):
+    host = q.PluginHost(width=32, height=32)
+    try:
+        scene = q.make_scene(spec, host.lib)
+        n = scene.tri_count
+        host.set_scene(scene)
+        g = host.read_bvh(n)
+        words = host.read_wide_bvh(n)
+        assert host.stats().error_flags == 0
+        host.set_options(bvh_cluster=1)
+        plain = host.read_bvh(n)
+    finally:
+        host.destroy()
+    o = orc.lbvh(scene.vertices)
+    assert np.array_equal(g["morton"], o["morton"]) and np.array_equal(g["order"], o["order"])
+    assert np.array_equal(plain["children"], o["children"])
+    ch = g["children"]
+    # every leaf once, every internal node but the root once
+    leaves = np.sort(~ch[ch < 0])
+    assert np.array_equal(leaves, np.arange(n))
+    inner = np.sort(ch[ch >= 0])
+    assert np.array_equal(inner, np.arange(1, n - 1))
+    # child boxes: exact unions of their triangles' boxes
+    tlo, thi = _tri_boxes(scene.vertices, g["order"])
+    sets = _leaf_sets(ch, n)
+    boxes = g["boxes"].reshape(-1, 2, 2, 3)
+    for c in range(n - 1):
+        for k in (0, 1):
+            x = int(ch[2 * c + k])
+            s = np.array([~x]) if x < 0 else sets[x]
+            assert np.array_equal(boxes[c, k, 0], tlo[s].min(axis=0)), (c, k)
+            assert np.array_equal(boxes[c, k, 1], thi[s].max(axis=0)), (c, k)
+    # the 8-wide records over the refined tree: every triangle in one reachable leaf, every
+    # decoded child box contains the boxes of what it holds
+    cover = np.zeros(n, np.int64)
+    for i in orc.wide_reachable(words):
+        for lo, hi, ref, internal in _decode(words, i):
+            if internal:
+                s = sets[ref]
+                assert s.size > 1
+            else:
+                xr = (~ref) & 0xFFFFFFFF
+                cnt = ((xr & 3) + 1) & 3
+                if cnt == 0:
+                    continue
+                s = np.arange(xr >> 2, (xr >> 2) + cnt)
+                cover[s] += 1
+            assert (lo <= tlo[s].min(axis=0)).all() and (hi >= thi[s].max(axis=0)).all()
+    assert (cover == 1).all()
+    if n > 100:
+        assert _area_sum(g["boxes"]) < _area_sum(plain["boxes"])
+
+
+def _render(spec: str, cluster: int, w: int, h: int, spp: int, depth: int):
+    host = q.PluginHost(width=w, height=h)
+    try:
+        host.set_scene(q.make_scene(spec, host.lib))
+        host.set_options(spp_per_frame=spp, max_depth=depth, seed=11, record_samples=1, collect_stats=1,
+                         bvh_cluster=cluster)
+        host.render(w, h, dirty=True)
+        img = np.array(host.readback())
+        aov = host.readback_aov()
+        rad, sig = host.read_samples(spp)
+        st = host.stats()
+        assert st.error_flags == 0
+        return img, aov, sig, st
+    finally:
+        host.destroy()
+
+
+@pytest.mark.parametrize("spec,w,h,spp,depth", [("cornell36", 64, 48, 8, 4), ("soup:n=100000,seed=5", 160, 90, 8, 6)])
+def test_refinement_leaves_images_identical(cuda_ok, spec, w, h, spp, depth):
+    a_img, a_aov, a_sig, a_st = _render(spec, 0, w, h, spp, depth)
+    b_img, b_aov, b_sig, b_st = _render(spec, 1, w, h, spp, depth)
+    assert np.array_equal(a_img, b_img)
+    for k in a_aov:
+        assert np.array_equal(a_aov[k], b_aov[k]), k
+    assert np.array_equal(a_sig, b_sig)
+    assert (a_st.camera_rays, a_st.extension_rays, a_st.shadow_rays) == (b_st.camera_rays, b_st.extension_rays,
+                                                                         b_st.shadow_rays)
+    if spec.startswith("soup"):
+        assert a_st.node_visits < b_st.node_visits  # the refined hierarchy is cheaper to traverse
