@@ -206,6 +206,9 @@ typedef struct Q_cuda_options {
     uint32_t bvh_cluster;        /* the LBVH's largest subtrees of at most this many leaves are
                                     rebuilt with the least surface-area split (0 = default 32;
                                     3..32; 1 or 2 = none: the plain Morton hierarchy) */
+    uint32_t bvh_collapse;       /* children of the 8-wide records: 0 = the spread of least
+                                    surface-area cost (default), 1 = the largest child opened
+                                    greedily */
 } Q_cuda_options;
 
 /* Counters of the last frame (rays actually traced) and of the whole accumulation. */

@@ -93,7 +93,7 @@ class Q_cuda_options(C.Structure):
                 ("trace_block", C.c_uint32), ("record_samples", C.c_uint32), ("collect_stats", C.c_uint32),
                 ("profile", C.c_uint32), ("megakernel", C.c_uint32), ("smem_levels", C.c_uint32),
                 ("ray_eps", C.c_float), ("refill_lanes", C.c_uint32), ("trace_steps", C.c_uint32),
-                ("bvh_width", C.c_uint32), ("bvh_cluster", C.c_uint32)]
+                ("bvh_width", C.c_uint32), ("bvh_cluster", C.c_uint32), ("bvh_collapse", C.c_uint32)]
 
 
 class Q_cuda_stats(C.Structure):

@@ -77,6 +77,9 @@ public:
     // Leaves of the largest subtrees rebuilt with the surface-area split after the Morton
     // hierarchy (3..32; below 3: the plain LBVH).
     void set_sah_cluster(int leaves) { sah_cluster_ = leaves < 3 ? 0 : (leaves > 32 ? 32 : leaves); }
+    // The 8-wide records' children from the surface-area-optimal spread (true) or by opening
+    // the largest child greedily (false).
+    void set_dp_collapse(bool on) { dp_collapse_ = on; }
 
     // Copies the top max_nodes internal nodes (breadth first) for staging in shared memory.
     cudaError_t build_treelet(int max_nodes, cudaStream_t stream, KernelProfiler& prof);
@@ -111,6 +114,9 @@ private:
     int sah_cluster_ = 32;           // leaves of the subtrees rebuilt with the SAH split (0: none)
     int* sah_roots_ = nullptr;       // roots of those subtrees
     int* sah_count_ = nullptr;
+    bool dp_collapse_ = true;
+    float* dp_cost_ = nullptr;       // 8 costs per internal node (k_collapse_dp)
+    uint8_t* dp_dec_ = nullptr;      // 8 decisions per internal node
     float4* tree_ = nullptr;
     int tree_n_ = 0;
     int tree_capacity_ = 0;

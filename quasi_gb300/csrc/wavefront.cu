@@ -218,6 +218,11 @@ int Renderer::set_options(const Q_cuda_options& o) {
         return fail(QUASI_ERR_INVALID, "bvh_width must be 0 (default), 2 or 8");
     if (n.bvh_cluster > 32) return fail(QUASI_ERR_INVALID, "bvh_cluster must be at most 32");
     if (n.bvh_cluster == 0) n.bvh_cluster = 32;
+    if (n.bvh_collapse > 1) return fail(QUASI_ERR_INVALID, "bvh_collapse must be 0 or 1");
+    if (n.bvh_collapse != opt_.bvh_collapse) {
+        bvh_.set_dp_collapse(n.bvh_collapse == 0);
+        bvh_dirty_ = true;
+    }
     const bool changed = n.seed != opt_.seed || n.max_depth != opt_.max_depth || n.integrator != opt_.integrator ||
                          n.ray_eps != opt_.ray_eps;
     if (n.bvh_cluster != opt_.bvh_cluster) {

@@ -15,7 +15,8 @@ pytestmark = pytest.mark.gpu
 @pytest.fixture(scope="module")
 def host(cuda_ok):
     h = q.PluginHost(width=32, height=32)
-    h.set_options(bvh_cluster=1)  # the plain Morton hierarchy (no surface-area refinement)
+    # the plain Morton hierarchy (no surface-area refinement), records by greedy opening
+    h.set_options(bvh_cluster=1, bvh_collapse=1)
     yield h
     h.destroy()
 

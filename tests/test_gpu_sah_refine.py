@@ -1,9 +1,10 @@
-"""Surface-area refinement of the LBVH (bvh_cluster): the largest subtrees of at most 32
-leaves are rebuilt with the least-cost split. Checked as a hierarchy (every leaf once, every
+"""Surface-area refinement of the LBVH (bvh_cluster: the largest subtrees of at most 32
+leaves rebuilt with the least-cost split) and the surface-area-optimal spread of the binary
+nodes over the 8-wide records (bvh_collapse). Checked as a hierarchy (every leaf once, every
 child box the exact union of its triangles' boxes, the 8-wide records covering and
-containing what they hold), as an improvement (lower surface-area sum, fewer record
-visits), and by its effect on images: none, since every hit decision is exact, so frames
-rendered over the refined and the plain hierarchy are identical bit for bit."""
+containing what they hold), as an improvement (lower surface-area sum, fewer records, fewer
+record visits), and by their effect on images: none, since every hit decision is exact, so
+frames rendered over the refined and the plain hierarchy are identical bit for bit."""
 from __future__ import annotations
 
 import numpy as np
@@ -56,7 +57,9 @@ def test_refined_hierarchy_is_valid_and_better(cuda_ok, orc, spec):
         g = host.read_bvh(n)
         words = host.read_wide_bvh(n)
         assert host.stats().error_flags == 0
-        host.set_options(bvh_cluster=1)
+        host.set_options(bvh_collapse=1)
+        greedy_words = host.read_wide_bvh(n)
+        host.set_options(bvh_cluster=1, bvh_collapse=1)
         plain = host.read_bvh(n)
     finally:
         host.destroy()
@@ -98,14 +101,22 @@ def test_refined_hierarchy_is_valid_and_better(cuda_ok, orc, spec):
     assert (cover == 1).all()
     if n > 100:
         assert _area_sum(g["boxes"]) < _area_sum(plain["boxes"])
+    # the spread over the records minimises the summed surface area of the records' boxes:
+    # no more than greedy opening of the same binary tree
+    node_lo, node_hi = boxes[:, :, 0].min(axis=1).astype(np.float64), boxes[:, :, 1].max(axis=1).astype(np.float64)
+    d = node_hi - node_lo
+    half = d[:, 0] * d[:, 1] + d[:, 1] * d[:, 2] + d[:, 2] * d[:, 0]
+    dp_cost = half[orc.wide_reachable(words)].sum()
+    greedy_cost = half[orc.wide_reachable(greedy_words)].sum()
+    assert dp_cost <= greedy_cost * (1 + 1e-6), (dp_cost, greedy_cost)
 
 
-def _render(spec: str, cluster: int, w: int, h: int, spp: int, depth: int):
+def _render(spec: str, cluster: int, collapse: int, w: int, h: int, spp: int, depth: int):
     host = q.PluginHost(width=w, height=h)
     try:
         host.set_scene(q.make_scene(spec, host.lib))
         host.set_options(spp_per_frame=spp, max_depth=depth, seed=11, record_samples=1, collect_stats=1,
-                         bvh_cluster=cluster)
+                         bvh_cluster=cluster, bvh_collapse=collapse)
         host.render(w, h, dirty=True)
         img = np.array(host.readback())
         aov = host.readback_aov()
@@ -119,13 +130,17 @@ def _render(spec: str, cluster: int, w: int, h: int, spp: int, depth: int):
 
 @pytest.mark.parametrize("spec,w,h,spp,depth", [("cornell36", 64, 48, 8, 4), ("soup:n=100000,seed=5", 160, 90, 8, 6)])
 def test_refinement_leaves_images_identical(cuda_ok, spec, w, h, spp, depth):
-    a_img, a_aov, a_sig, a_st = _render(spec, 0, w, h, spp, depth)
-    b_img, b_aov, b_sig, b_st = _render(spec, 1, w, h, spp, depth)
-    assert np.array_equal(a_img, b_img)
-    for k in a_aov:
-        assert np.array_equal(a_aov[k], b_aov[k]), k
-    assert np.array_equal(a_sig, b_sig)
-    assert (a_st.camera_rays, a_st.extension_rays, a_st.shadow_rays) == (b_st.camera_rays, b_st.extension_rays,
-                                                                         b_st.shadow_rays)
+    runs = [_render(spec, cl, co, w, h, spp, depth) for cl, co in ((0, 0), (1, 0), (1, 1))]
+    a_img, a_aov, a_sig, a_st = runs[0]
+    for b_img, b_aov, b_sig, b_st in runs[1:]:
+        assert np.array_equal(a_img, b_img)
+        for k in a_aov:
+            assert np.array_equal(a_aov[k], b_aov[k]), k
+        assert np.array_equal(a_sig, b_sig)
+        assert (a_st.camera_rays, a_st.extension_rays, a_st.shadow_rays) == (b_st.camera_rays, b_st.extension_rays,
+                                                                             b_st.shadow_rays)
     if spec.startswith("soup"):
-        assert a_st.node_visits < b_st.node_visits  # the refined hierarchy is cheaper to traverse
+        # each step is cheaper to traverse: refined + optimal spread, plain + optimal spread,
+        # plain + greedy opening
+        visits = [r[3].node_visits for r in runs]
+        assert visits[0] < visits[1] < visits[2], visits
