@@ -300,7 +300,8 @@ constexpr int k_mode_wide_refill = 4; // per-lane refill over the 8-wide records
 // k_batch_shade (a register cap). Before the shading table k_shade took 141 registers
 // uncapped and the 1080p frame's shading cost 138 ms; 2 blocks (128 registers) or 4 (64,
 // with spills) cost 101 ms on GB300. With the continuation finished before the light sample
-// (shade_and_enqueue) it fits 80 registers without spills at 3 blocks.
+// (shade_and_enqueue) it fits 78 registers without spills at 3 blocks; 4 blocks (64
+// registers, 36 bytes spilled) cost 20 % more (33.6 vs 40.2 ms per 1080p frame).
 #ifndef QUASI_SHADE_MIN_BLOCKS
 #define QUASI_SHADE_MIN_BLOCKS 3
 #endif
