@@ -343,7 +343,7 @@ int BatchRenderer::record_frame(cudaStream_t s, uint32_t& launches) {
                     : (wide ? k_batch_trace_shadow<false, true> : k_batch_trace_shadow<false, false>);
     auto km = stats ? k_batch_megakernel<true> : k_batch_megakernel<false>;
     const int grid_c = grid_c_, grid_s = grid_s_, grid_m = grid_m_;
-    const int grid_shade = sm * 8;
+    const int grid_shade = sm * 32;  // as the single-scene renderer's shading launch
     int occ_f = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, k_batch_fixup<ClosestJob>, 128, 0);
     const int grid_fixup = sm * std::max(occ_f, 1);
