@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(256, QUASI_SHADE_MIN_BLOCKS) k_batch_shade(con
             h = hits[i];
             pid = __float_as_int(h.z);
             if (__float_as_int(h.y) < 0) {
-                if (p.sig) p.sig[pid] = sig_mix(p.sig[pid], k_sig_miss);
+                miss_at_bounce(p, bounce, pid);
             } else {
                 m = meta[pid];
             }

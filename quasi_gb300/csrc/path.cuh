@@ -168,10 +168,9 @@ __device__ __forceinline__ bool begin_path(const FrameParams& f, const PathDev& 
     d = ff3_f(rd);
     const float te = n_tris ? scene_entry(nodes, f.cam.origin, d) : 0.0f;
     o = te > 0.0f ? ff3_f(ff3_add(ro, ff3_scale(rd, te))) : f.cam.origin;  // as ExactShifted
-    p.beta[pid] = make_float4(1.f, 1.f, 1.f, 0.f);
+    // beta starts at 1 and the first-hit AOVs at 0 without being stored: shading at bounce 1
+    // takes beta as 1 and writes the AOVs of every path, hit or missed (miss_at_bounce)
     p.lpath[pid] = make_float4(0.f, 0.f, 0.f, te);
-    p.aov_a[pid] = make_float4(0.f, 0.f, 0.f, 0.f);
-    p.aov_n[pid] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (p.sig) p.sig[pid] = 0u;
     return true;
 }
@@ -296,6 +295,16 @@ constexpr int k_mode_refill = 2;      // per-lane refill (trace_persistent)
 constexpr int k_mode_wide = 3;        // warp batches over the 8-wide records (trace_batches_wide)
 constexpr int k_mode_wide_refill = 4; // per-lane refill over the 8-wide records (trace_wide_refill)
 
+// A path whose closest-hit ray of bounce `bounce` missed: its signature, and at bounce 1 the
+// zero first-hit AOVs the camera kernel leaves unwritten.
+__device__ __forceinline__ void miss_at_bounce(const PathDev& p, uint32_t bounce, int pid) {
+    if (p.sig) p.sig[pid] = sig_mix(p.sig[pid], k_sig_miss);
+    if (bounce == 1) {
+        p.aov_a[pid] = make_float4(0.f, 0.f, 0.f, 0.f);
+        p.aov_n[pid] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
 // Minimum resident 256-thread blocks per SM asked of the compiler for k_shade and
 // k_batch_shade (a register cap). Before the shading table k_shade took 141 registers
 // uncapped and the 1080p frame's shading cost 138 ms; 2 blocks (128 registers) or 4 (64,
@@ -332,7 +341,7 @@ __device__ __forceinline__ void shade_and_enqueue(bool active, const FrameParams
         slot_to_xy(local - j * f.slots, f.tiles_x, px, py);
         r = vertex_random(path_key(f.seed, py * f.width + px, f.sample_base + j, bounce));
         const float3 alb = xyz(__ldg(&s.albedo[prim]));
-        nb = xyz(p.beta[pid]) * alb;
+        nb = bounce == 1 ? alb : xyz(p.beta[pid]) * alb;  // beta is 1 at the first hit (1 * a = a)
         cont = bounce < f.max_depth && max3(nb) > 0.0f;
         vertex_point(vs, prim, ro, rd, x, nrm);
         org = vertex_origin(vs, x, nrm);

@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(256, QUASI_SHADE_MIN_BLOCKS) k_shade(FramePara
         if (i < n) {
             h = hits[i];
             pid = __float_as_int(h.z);
-            if (__float_as_int(h.y) < 0 && p.sig) p.sig[pid] = sig_mix(p.sig[pid], k_sig_miss);
+            if (__float_as_int(h.y) < 0) miss_at_bounce(p, bounce, pid);
         }
         shade_and_enqueue(i < n && __float_as_int(h.y) >= 0, f, s, p, bounce, pid, static_cast<uint32_t>(pid), h,
                           shadow_q, shadow_count, next_q, next_count);
