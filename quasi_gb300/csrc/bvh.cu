@@ -509,10 +509,23 @@ __global__ void __launch_bounds__(256) k_sah_rebuild(const float4* __restrict__ 
             }
             const uint2 task = s_task[warp][--n_task];
             const uint32_t mask = task.x;
+            float bl[6], br[6];
+            uint32_t left;
+            if (__popc(mask) == 2) {
+                // two leaves: one split, no search (half the nodes of a subtree)
+                const int l0 = __ffs(mask) - 1, l1 = __ffs(mask & (mask - 1u)) - 1;
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    bl[a] = __shfl_sync(0xffffffffu, lo[a], l0);
+                    bl[3 + a] = __shfl_sync(0xffffffffu, hi[a], l0);
+                    br[a] = __shfl_sync(0xffffffffu, lo[a], l1);
+                    br[3 + a] = __shfl_sync(0xffffffffu, hi[a], l1);
+                }
+                left = 1u << l0;
+            } else {
             // best split over the three axes: leaves of rank <= r go left
             float best = __int_as_float(0x7f800000);
             int best_axis = 0, best_r = 0;
-            float bl[6], br[6];
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 const bool member = (mask >> s_lane[warp][k][lane]) & 1u;
@@ -571,7 +584,8 @@ __global__ void __launch_bounds__(256) k_sah_rebuild(const float4* __restrict__ 
                 break;
             }
             const bool mine = (mask >> lane) & 1u;
-            const uint32_t left = __ballot_sync(0xffffffffu, mine && rank[best_axis] <= best_r);
+            left = __ballot_sync(0xffffffffu, mine && rank[best_axis] <= best_r);
+            }
             const uint32_t right = mask & ~left;
             const uint32_t side[2] = {left, right};
             const int need = (__popc(left) > 1 ? 1 : 0) + (__popc(right) > 1 ? 1 : 0);
