@@ -19,9 +19,13 @@
 namespace quasi {
 
 // Camera basis (plugin.mm:134-147) as double-float vectors, split on the host from double.
+// Camera basis as double-float vectors (hi, lo): the unnormalised direction of pixel
+// position (x + jx, y + jy) is base + step_x (x + jx) - step_y (y + jy), with
+// base = lower-left corner + vertical - origin, step_x = horizontal / width and
+// step_y = vertical / height (plugin.mm:134-153 with u = (x + jx) / W, v = 1 - (y + jy) / H).
 struct CameraFF {
     float3 origin;
-    float3 ll_hi, ll_lo, h_hi, h_lo, v_hi, v_lo;
+    float3 base_hi, base_lo, sx_hi, sx_lo, sy_hi, sy_lo;
 };
 
 struct FrameParams {
@@ -115,17 +119,17 @@ __device__ __forceinline__ void warp_add_count(int v, unsigned long long* out) {
 }
 
 // Camera ray of (pixel x,y; sample) in double-float: jitter (r1, r2) inside the pixel,
-// u = (x + r1) / W, v = 1 - (y + r2) / H, direction = normalize(ll + u h + v v' - o).
+// u = (x + r1) / W, v = 1 - (y + r2) / H, direction = normalize(ll + u h + v v' - o), as
+// base + step_x (x + r1) - step_y (y + r2) with the per-frame vectors of CameraFF.
 __device__ __forceinline__ void camera_ray_ff(const FrameParams& f, uint32_t x, uint32_t y, uint32_t sample, ff3& o,
                                               ff3& d) {
     uint32_t st = path_key(f.seed, y * f.width + x, sample, 0u);
     const float jx = rng_next(st);
     const float jy = rng_next(st);
-    const ff u = ff_div(two_sum(static_cast<float>(x), jx), ffv(static_cast<float>(f.width)));
-    const ff v = ff_sub(ffv(1.0f), ff_div(two_sum(static_cast<float>(y), jy), ffv(static_cast<float>(f.height))));
-    d = ff3_normalize(ff3_sub(ff3_add(ff3_add(ff3_pair(f.cam.ll_hi, f.cam.ll_lo), ff3_scale(ff3_pair(f.cam.h_hi, f.cam.h_lo), u)),
-                                      ff3_scale(ff3_pair(f.cam.v_hi, f.cam.v_lo), v)),
-                              ff3v(f.cam.origin)));
+    const ff px = two_sum(static_cast<float>(x), jx), py = two_sum(static_cast<float>(y), jy);
+    d = ff3_normalize(ff3_sub_fast(ff3_add_fast(ff3_pair(f.cam.base_hi, f.cam.base_lo),
+                                                ff3_scale(ff3_pair(f.cam.sx_hi, f.cam.sx_lo), px)),
+                                   ff3_scale(ff3_pair(f.cam.sy_hi, f.cam.sy_lo), py)));
     o = ff3v(f.cam.origin);
 }
 

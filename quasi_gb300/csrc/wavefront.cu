@@ -39,20 +39,24 @@ CameraFF make_camera_basis(const Q_camera& c, uint32_t w, uint32_t h) {
     const double vw = (double(w) / double(h)) * vh;
     CameraFF b;
     b.origin = make_float3(c.position[0], c.position[1], c.position[2]);
-    double H[3], V[3], LL[3];
+    // ll + u h + v vv - o with u = px / w, v = 1 - py / h is
+    // (ll + vv - o) + (h / w) px - (vv / h) py
+    double base[3], sx[3], sy[3];
     for (int k = 0; k < 3; ++k) {
-        H[k] = vw * r[k];
-        V[k] = vh * u2[k];
-        LL[k] = double(c.position[k]) - H[k] * 0.5 - V[k] * 0.5 - wv[k];
+        const double H = vw * r[k], V = vh * u2[k];
+        const double LL = double(c.position[k]) - H * 0.5 - V * 0.5 - wv[k];
+        base[k] = LL + V - double(c.position[k]);
+        sx[k] = H / double(w);
+        sy[k] = V / double(h);
     }
     // Each double splits into hi = nearest float and lo = nearest float of the remainder.
     auto split = [](const double* d, float3& hi, float3& lo) {
         hi = make_float3(float(d[0]), float(d[1]), float(d[2]));
         lo = make_float3(float(d[0] - double(hi.x)), float(d[1] - double(hi.y)), float(d[2] - double(hi.z)));
     };
-    split(H, b.h_hi, b.h_lo);
-    split(V, b.v_hi, b.v_lo);
-    split(LL, b.ll_hi, b.ll_lo);
+    split(base, b.base_hi, b.base_lo);
+    split(sx, b.sx_hi, b.sx_lo);
+    split(sy, b.sy_hi, b.sy_lo);
     return b;
 }
 
