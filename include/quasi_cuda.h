@@ -228,8 +228,10 @@ typedef struct Q_cuda_stats {
     double bvh_ms;            /* device time of the last LBVH build */
     uint64_t adjoint_rays;    /* rays replayed by Q_cuda_backward since the plugin was created */
     uint64_t redecided_rays;  /* rays of the last frame that met a triangle test the FP32 error
-                                 bound could not decide and were re-traced with exact
-                                 (double-float) decisions (wavefront form; 0 otherwise) */
+                                 bound could not decide: the fixup kernels re-decided their one
+                                 undecided candidate in double-float, or re-traced the ray with
+                                 exact decisions when it met several (wavefront form; 0
+                                 otherwise) */
 } Q_cuda_stats;
 
 #define QUASI_DEVERR_STACK     1u
@@ -399,8 +401,9 @@ typedef struct Q_cuda_batch_stats {
     uint64_t px_total;          /* pixels of all scenes (the batch image pool) */
     double frame_ms;            /* device time of the last frame */
     uint64_t adjoint_rays;      /* rays replayed by Q_cuda_batch_backward since the last reset */
-    uint64_t redecided_rays;    /* rays re-traced with exact decisions (wavefront form), since the
-                                   last reset */
+    uint64_t redecided_rays;    /* rays with an undecided triangle test, re-decided by the
+                                   fixup kernels as in Q_cuda_stats (wavefront form), since
+                                   the last reset */
 } Q_cuda_batch_stats;
 
 /* Uploads the scenes and builds their LBVHs. *out receives the batch; on failure returns
