@@ -212,6 +212,21 @@ __device__ __forceinline__ ff ff3_dot(const ff3& a, const ff3& b) {
 __device__ __forceinline__ ff ff3_dot_fast(const ff3& a, const ff3& b) {
     return ff_add_fast(ff_add_fast(ff_mul(a.x, b.x), ff_mul(a.y, b.y)), ff_mul(a.z, b.z));
 }
+// a . b - c rounded to float. The products of the high parts and their sums are formed exactly
+// (TwoProd, TwoSum); only the low-order terms (product and sum errors, cross terms with the
+// low parts) are added in FP32. The absolute error stays near 2^-48 (|a||b| + |c|) however much
+// the terms cancel, so a result near zero keeps its relative accuracy.
+__device__ __forceinline__ float ff3_dot_sub(const ff3& a, const ff3& b, float c) {
+    const ff px = two_prod(a.x.hi, b.x.hi), py = two_prod(a.y.hi, b.y.hi), pz = two_prod(a.z.hi, b.z.hi);
+    const ff s1 = two_sum(px.hi, py.hi);
+    const ff s2 = two_sum(s1.hi, pz.hi);
+    const ff s3 = two_sum(s2.hi, -c);
+    float lo = __fadd_rn(__fadd_rn(__fadd_rn(px.lo, py.lo), __fadd_rn(pz.lo, s1.lo)), __fadd_rn(s2.lo, s3.lo));
+    lo = __fmaf_rn(a.x.hi, b.x.lo, __fmaf_rn(a.x.lo, b.x.hi, lo));
+    lo = __fmaf_rn(a.y.hi, b.y.lo, __fmaf_rn(a.y.lo, b.y.hi, lo));
+    lo = __fmaf_rn(a.z.hi, b.z.lo, __fmaf_rn(a.z.lo, b.z.hi, lo));
+    return __fadd_rn(s3.hi, lo);
+}
 __device__ __forceinline__ ff3 ff3_cross(const ff3& a, const ff3& b) {
     return ff3{ff_sub(ff_mul(a.y, b.z), ff_mul(a.z, b.y)), ff_sub(ff_mul(a.z, b.x), ff_mul(a.x, b.z)),
                ff_sub(ff_mul(a.x, b.y), ff_mul(a.y, b.x))};

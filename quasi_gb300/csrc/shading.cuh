@@ -161,19 +161,22 @@ __device__ __forceinline__ void vertex_light(const VertexScene& s, int prim, con
     // (y - x) first, in double-float: both lie on their planes, so a small surface-to-light
     // gap keeps its digits; subtracting the rounded offset origin would not. The light sample
     // only weights this vertex (nothing of it carries to the next bounce), so once that
-    // difference is formed the eps offset, length, direction and cosines are FP32: relative
-    // errors ~1e-7 against the 1e-4 bound.
-    const float3 d0 = ff3_f(ff3_sub_fast(yl, x));
+    // difference is formed the eps offset and the length are FP32 (relative errors ~1e-7).
+    const ff3 dxy = ff3_sub_fast(yl, x);
+    const float3 d0 = ff3_f(dxy);
     const float3 nf = ff3_f(nrm);
     const float3 dv = mk3(__fsub_rn(d0.x, __fmul_rn(s.eps, nf.x)), __fsub_rn(d0.y, __fmul_rn(s.eps, nf.y)),
                           __fsub_rn(d0.z, __fmul_rn(s.eps, nf.z)));
     const float d2 = fdot3(dv, dv);
     const float inv_dist = __fdiv_rn(1.0f, __fsqrt_rn(d2));
-    const float3 wi = mk3(__fmul_rn(dv.x, inv_dist), __fmul_rn(dv.y, inv_dist), __fmul_rn(dv.z, inv_dist));
-    const float cos_x = fdot3(ff3_f(nrm), wi);
+    // The cosines are not: an FP32 dot of unit vectors keeps an absolute error of ~1e-7, a
+    // relative error above 1e-4 once a grazing light sample brings a cosine below ~1e-3. Both
+    // come from the double-float difference with exact products and sums instead:
+    // n.dv = n.(y - x) - eps (n is a unit vector) and nl.dv = nl.(y - x) - eps (nl.n).
     const ff area2 = ff{lt.v1.w, lt.v2.w};
     const ff3 nl = ff3{ff{lt.n0.x, lt.n0.y}, ff{lt.n0.z, lt.n0.w}, ff{lt.n1.x, lt.n1.y}};
-    const float cl = fdot3(ff3_f(nl), wi);
+    const float cos_x = __fmul_rn(ff3_dot_sub(nrm, dxy, s.eps), inv_dist);
+    const float cl = __fmul_rn(ff3_dot_sub(nl, dxy, __fmul_rn(s.eps, fdot3(ff3_f(nl), nf))), inv_dist);
     const float cos_l = fabsf(cl);
     if (cos_x > 0.0f && cos_l > 0.0f && d2 > 0.0f) {
         out.g = cos_x * cos_l / d2 * (0.5f * ff_f(area2)) * static_cast<float>(s.n_emit) * k_inv_pi;

@@ -24,7 +24,8 @@ static long double val(ff a) { return (long double)a.hi + (long double)a.lo; }
 int main() {
     std::mt19937_64 rng(7);
     std::uniform_real_distribution<double> U(-2.0, 2.0), P(1e-3, 4.0), R01(0.0, 1.0);
-    long double e_add = 0, e_addf = 0, e_mul = 0, e_div = 0, e_sqrt = 0, e_sin = 0, e_cos = 0;
+    long double e_add = 0, e_addf = 0, e_mul = 0, e_div = 0, e_sqrt = 0, e_sin = 0, e_cos = 0, e_dotsub = 0;
+    std::uniform_real_distribution<double> LogD(-12.0, 0.0);
     auto mk = [&](double d) { ff x; x.hi = (float)d; x.lo = (float)(d - (double)x.hi); return x; };
     for (int i = 0; i < 200000; ++i) {
         const ff a = mk(U(rng)), b = mk(U(rng)), p = mk(P(rng));
@@ -44,8 +45,28 @@ int main() {
         const long double pi = 3.141592653589793238462643383279502884L;
         e_sin = fmaxl(e_sin, fabsl(val(s) - sinl(pi * (long double)x)));
         e_cos = fmaxl(e_cos, fabsl(val(c) - cosl(pi * (long double)x)));
+        // a . b - c for a unit a and a b nearly orthogonal to it (a grazing cosine): beyond the
+        // final rounding to float (2^-24 of the result) the error must stay near 2^-48 of the
+        // terms' magnitudes, however small the result
+        {
+            const double ux = U(rng), uy = U(rng), uz = U(rng), ul = std::sqrt(ux * ux + uy * uy + uz * uz) + 1e-9;
+            const double nx = ux / ul, ny = uy / ul, nz = uz / ul;
+            double tx = U(rng), ty = U(rng), tz = U(rng);
+            const double tn = tx * nx + ty * ny + tz * nz, delta = std::pow(10.0, LogD(rng));
+            tx += (delta - tn) * nx;
+            ty += (delta - tn) * ny;
+            tz += (delta - tn) * nz;
+            const quasi::ff3 na{mk(nx), mk(ny), mk(nz)}, tb{mk(tx), mk(ty), mk(tz)};
+            const float cc = (i & 1) ? 1e-4f : 0.0f;
+            const long double terms[3] = {val(na.x) * val(tb.x), val(na.y) * val(tb.y), val(na.z) * val(tb.z)};
+            const long double want = terms[0] + terms[1] + terms[2] - (long double)cc;
+            const long double mag = fabsl(terms[0]) + fabsl(terms[1]) + fabsl(terms[2]) + fabsl((long double)cc);
+            const long double got = quasi::ff3_dot_sub(na, tb, cc);
+            const long double beyond = fabsl(got - want) - 0x1p-24L * fabsl(want);
+            e_dotsub = fmaxl(e_dotsub, fmaxl(beyond, 0.0L) / mag);
+        }
     }
-    std::printf("add %.3Le\naddf %.3Le\nmul %.3Le\ndiv %.3Le\nsqrt %.3Le\nsin %.3Le\ncos %.3Le\n", e_add, e_addf,
-                e_mul, e_div, e_sqrt, e_sin, e_cos);
+    std::printf("add %.3Le\naddf %.3Le\nmul %.3Le\ndiv %.3Le\nsqrt %.3Le\nsin %.3Le\ncos %.3Le\ndotsub %.3Le\n", e_add,
+                e_addf, e_mul, e_div, e_sqrt, e_sin, e_cos, e_dotsub);
     return 0;
 }

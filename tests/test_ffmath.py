@@ -15,7 +15,7 @@ def test_double_float_operations_are_accurate(tmp_path):
                     str(ROOT / "tests" / "ffmath_check.cpp"), "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
     errs = {k: float(v) for k, v in (line.split() for line in out.splitlines())}
-    assert set(errs) == {"add", "addf", "mul", "div", "sqrt", "sin", "cos"}
+    assert set(errs) == {"add", "addf", "mul", "div", "sqrt", "sin", "cos", "dotsub"}
     for k, v in errs.items():
         assert v < 5e-14, (k, v)
 
