@@ -302,18 +302,13 @@ void BatchRenderer::compute_grids() {
                     : (wide ? k_batch_trace_shadow<false, true> : k_batch_trace_shadow<false, false>);
     auto km = stats ? k_batch_megakernel<true> : k_batch_megakernel<false>;
     const int tb = static_cast<int>(opt_.trace_block), mb = std::min(tb, 128);
-    int occ_c = 0, occ_s = 0, occ_m = 0, occ_a = 0;
     smem_c_ = wide ? wide_stack_smem_bytes<false>(tb) : 0;
     smem_s_ = wide ? wide_stack_smem_bytes<true>(tb) : 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, kc, tb, smem_c_);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, ks, tb, smem_s_);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_m, km, mb, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, k_batch_adjoint, 128, 0);
     const int sm = owner_.sm_count();
-    grid_c_ = sm * std::max(occ_c, 1);
-    grid_s_ = sm * std::max(occ_s, 1);
-    grid_m_ = sm * std::max(occ_m, 1);
-    grid_adj_ = sm * std::max(occ_a, 1);
+    grid_c_ = sm * resident_blocks(kc, tb, smem_c_);
+    grid_s_ = sm * resident_blocks(ks, tb, smem_s_);
+    grid_m_ = sm * resident_blocks(km, mb, 0);
+    grid_adj_ = sm * resident_blocks(k_batch_adjoint, 128, 0);
 }
 
 // Enqueues one frame (every wave of the plan) on s; `launches` receives the kernel count.
@@ -344,9 +339,7 @@ int BatchRenderer::record_frame(cudaStream_t s, uint32_t& launches) {
     auto km = stats ? k_batch_megakernel<true> : k_batch_megakernel<false>;
     const int grid_c = grid_c_, grid_s = grid_s_, grid_m = grid_m_;
     const int grid_shade = sm * 32;  // as the single-scene renderer's shading launch
-    int occ_f = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, k_batch_fixup<ClosestJob>, 128, 0);
-    const int grid_fixup = sm * std::max(occ_f, 1);
+    const int grid_fixup = sm * resident_blocks(k_batch_fixup<ClosestJob>, 128, 0);
     const int cap = static_cast<int>(wave_capacity_);
     for (size_t w = 0; w < waves_.size(); ++w) {
         const Wave& wv = waves_[w];

@@ -29,6 +29,21 @@ inline uint64_t wave_paths_fitting(uint64_t want, size_t bytes_per_path, size_t 
     return fit < want ? fit : want;
 }
 
+// Resident blocks per SM of `kernel` launched with `threads` threads and `smem` bytes of
+// dynamic shared memory, at least 1. The persistent kernels size their grids with it; they
+// loop over their work, so a grid of one block per SM (the answer if the query itself fails,
+// whose error is then cleared so a later launch check does not report it) is slower, never
+// wrong.
+template <class Kernel>
+int resident_blocks(Kernel kernel, int threads, size_t smem) {
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    return occ > 1 ? occ : 1;
+}
+
 // NVTX range over a host scope (frame, LBVH build, wave): lets a profiler attribute and
 // filter the launches inside it (ncu --nvtx --nvtx-include "quasi.wave/"). Without an
 // attached tool the calls return at once.

@@ -432,11 +432,8 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
     const bool shared_stacks = mode == k_mode_wide_refill;
     const size_t smem_c = shared_stacks ? wide_stack_smem_bytes<false>(tb) : tree_smem;
     const size_t smem_s = shared_stacks ? wide_stack_smem_bytes<true>(tb) : tree_smem;
-    int occ_c = 0, occ_s = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, kc, tb, smem_c);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, ks, tb, smem_s);
-    const int grid_c = sm_count_ * std::max(occ_c, 1);
-    const int grid_s = sm_count_ * std::max(occ_s, 1);
+    const int grid_c = sm_count_ * resident_blocks(kc, tb, smem_c);
+    const int grid_s = sm_count_ * resident_blocks(ks, tb, smem_s);
 // Blocks per SM of the shading launch (grid-stride over the hits, 3 resident per SM): 3, 8,
 // 16, 32 and 64 gave 34.8, 33.6, 32.8, 32.3 and 32.4 ms per 1080p frame.
 #ifndef QUASI_SHADE_GRID_PER_SM
@@ -445,9 +442,7 @@ int Renderer::render_wavefront(cudaStream_t s, uint32_t spp) {
     const int grid_shade = sm_count_ * QUASI_SHADE_GRID_PER_SM;
     // The fixup kernels are latency-bound (dependent loads, then double-float arithmetic):
     // as many blocks as fit.
-    int occ_f = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, k_fixup<ClosestJob>, 128, 0);
-    const int grid_fixup = sm_count_ * std::max(occ_f, 1);
+    const int grid_fixup = sm_count_ * resident_blocks(k_fixup<ClosestJob>, 128, 0);
     uint32_t* err = err_dev_.as<uint32_t>();
     unsigned long long* st = stats_dev_.as<unsigned long long>();
     const uint32_t px = width_ * height_;
@@ -555,10 +550,8 @@ int Renderer::render_megakernel(cudaStream_t s, uint32_t spp) {
     PathDev pd{beta_.as<float4>(),  lpath_.as<float4>(), aov_a_.as<float4>(),
                aov_n_.as<float4>(), ray_ff_.as<float4>(), opt_.record_samples ? sig_.as<uint32_t>() : nullptr};
     FrameParams f = frame_params(spp, slots, tiles_x);
-    int occ = 0;
     auto kern = opt_.collect_stats ? k_megakernel<true> : k_megakernel<false>;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 128, 0);
-    const int grid = sm_count_ * std::max(occ, 1);
+    const int grid = sm_count_ * resident_blocks(kern, 128, 0);
     unsigned long long* st = stats_dev_.as<unsigned long long>();
     const uint32_t px = width_ * height_;
     for (uint32_t w = 0; w < waves; ++w) {
@@ -626,9 +619,7 @@ int Renderer::backward(const float* grad_image, uint32_t spp, uint32_t sample_ba
     f.wave_offset = 0;
     const SceneDev sd = Renderer_scene_dev(bvh_.view(), tri_in_, albedo_, emission_, n_tris_, n_emit_,
                                            opt_.bvh_width);
-    int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_adjoint, 128, 0);
-    const int grid = sm_count_ * std::max(occ, 1);
+    const int grid = sm_count_ * resident_blocks(k_adjoint, 128, 0);
     R_TRY(QUASI_LAUNCH(prof_, "adjoint", s,
                        (k_adjoint<<<grid, 128, 0, s>>>(f, sd, grad_image, 1.0f / static_cast<float>(spp), grad_albedo,
                                                       grad_emission, counters_.as<int>(), err_dev_.as<uint32_t>(),
