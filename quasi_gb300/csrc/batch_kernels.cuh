@@ -158,7 +158,7 @@ __device__ __forceinline__ void trace_wide_refill_multi(Job& job, const BatchSce
         bool done = false;
         if (active) {
 #pragma unroll 1
-            for (int i = 0; i < k_wide_visits_per_check; ++i) {
+            for (int i = 0; i < wide_visits_per_check<ANY>(); ++i) {
                 done = wide_visit<ANY, STATS>(wide, tris, q, stack, err, cnt);
                 if (done) break;
             }

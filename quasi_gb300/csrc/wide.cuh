@@ -114,11 +114,23 @@ __device__ __forceinline__ int2* wide_stack_slot() {
     return s_wide_stack + (threadIdx.x >> 5) * (32 * wide_smem_stack<ANY>()) + (threadIdx.x & 31);
 }
 
-// Record visits a lane makes between two refill checks of its warp (ballot, fetch, vote).
-// Checking after every visit spends issue slots on the votes; after every second visit a
-// lane whose ray ended idles for at most one visit. 1080p frame of the 1M soup: 1 visit
-// 1420 Mrays/s, 2: 1444, 3: 1429, 4: 1437 (closest-hit 1 and any-hit 2: 1422).
-constexpr int k_wide_visits_per_check = 2;
+// Record visits a lane makes between two refill checks of its warp (ballot, fetch, vote),
+// for closest-hit and for any-hit rays. Checking after every visit spends issue slots on the
+// votes; after every k-th visit a lane whose ray ended idles for at most k - 1 visits. 1080p
+// frame of the 1M soup, both kinds alike: 1 visit 1420 Mrays/s, 2: 1444, 3: 1429, 4: 1437.
+// With the refined hierarchy and closest-hit at 2, any-hit at 1, 2, 3, 4, 5, 6: shadow traces
+// of 113.5, 111.5, 109.9, 108.4, 109.5 and 110.5 ms per frame (1547.5 Mrays/s at 4);
+// closest-hit at 3 (any-hit 3) took 299.4 instead of 296.5 ms.
+#ifndef QUASI_WIDE_VISITS_PER_CHECK
+#define QUASI_WIDE_VISITS_PER_CHECK 2
+#endif
+#ifndef QUASI_WIDE_VISITS_PER_CHECK_ANY
+#define QUASI_WIDE_VISITS_PER_CHECK_ANY 4
+#endif
+template <bool ANY>
+__host__ __device__ constexpr int wide_visits_per_check() {
+    return ANY ? QUASI_WIDE_VISITS_PER_CHECK_ANY : QUASI_WIDE_VISITS_PER_CHECK;
+}
 
 // Marks a finished traversal in WideRay::node (no record index is negative).
 constexpr int k_wide_done = static_cast<int>(0x80000000u);
@@ -455,7 +467,7 @@ __device__ __forceinline__ void trace_wide_refill(Job& job, const float4* __rest
         bool done = false;
         if (active) {
 #pragma unroll 1
-            for (int i = 0; i < k_wide_visits_per_check; ++i) {
+            for (int i = 0; i < wide_visits_per_check<ANY>(); ++i) {
                 done = wide_visit<ANY, STATS>(wide, tris, q, stack, err, cnt);
                 if (done) break;
             }
