@@ -209,7 +209,14 @@ typedef struct Q_cuda_options {
     uint32_t bvh_collapse;       /* children of the 8-wide records: 0 = the spread of least
                                     surface-area cost (default), 1 = the largest child opened
                                     greedily */
+    uint32_t bvh_split;          /* percentage of the triangles whose boxes are split in two
+                                    leaf references before the LBVH is built, the ones whose
+                                    boxes leave the most surface area empty (0 = default 30;
+                                    1..100; QUASI_BVH_SPLIT_NONE = none: leaf i is the
+                                    triangle at Morton position i, as the oracle builds it) */
 } Q_cuda_options;
+
+#define QUASI_BVH_SPLIT_NONE 0xFFFFFFFFu
 
 /* Counters of the last frame (rays actually traced) and of the whole accumulation. */
 typedef struct Q_cuda_stats {
@@ -273,7 +280,9 @@ Q_CUDA_EXPORT int Q_cuda_kernel_times(Q_plugin_handle* handle, Q_cuda_kernel_tim
                                       uint32_t capacity, uint32_t* count);
 Q_CUDA_EXPORT const char* Q_cuda_last_error(Q_plugin_handle* handle);
 
-/* Copies the current LBVH to host arrays (any pointer may be NULL). n = tri_count.
+/* Copies the current LBVH to host arrays (any pointer may be NULL). n = tri_count. Only
+ * without split references (bvh_split = QUASI_BVH_SPLIT_NONE; QUASI_ERR_STATE otherwise), so
+ * that its leaves are the triangles.
  *   morton    [n]        30-bit Morton code per triangle, original order
  *   order     [n]        original triangle index of each sorted position
  *   children  [2*(n-1)]  per internal node: child >= 0 internal node, child < 0 leaf ~pos
@@ -282,7 +291,8 @@ Q_CUDA_EXPORT const char* Q_cuda_last_error(Q_plugin_handle* handle);
 Q_CUDA_EXPORT int Q_cuda_read_bvh(Q_plugin_handle* handle, uint32_t* morton, uint32_t* order,
                                   int32_t* children, float* boxes, float* bounds);
 /* Copies the 8-wide traversal records collapsed from the LBVH: 24 words (96 bytes) per
- * internal node (max(n - 1, 1) records; layout in csrc/wide.cuh). Record 0 is the root; only
+ * internal node (max(n - 1, 1) records; layout in csrc/wide.cuh); like Q_cuda_read_bvh, only
+ * without split references. Record 0 is the root; only
  * records reachable from it through internal child references are used. No reference
  * counterpart: the reference traces by brute force (plugin.mm:199-212). */
 Q_CUDA_EXPORT int Q_cuda_read_wide_bvh(Q_plugin_handle* handle, uint32_t* words);

@@ -27,6 +27,8 @@ QUASI_ERR_TOO_LARGE = -7
 QUASI_INTEGRATOR_NEE = 0
 QUASI_INTEGRATOR_REFERENCE = 1
 
+QUASI_BVH_SPLIT_NONE = 0xFFFFFFFF
+
 QUASI_DEVERR_STACK = 1
 QUASI_DEVERR_TIMEOUT = 2
 QUASI_DEVERR_TRAVERSAL = 4
@@ -93,7 +95,8 @@ class Q_cuda_options(C.Structure):
                 ("trace_block", C.c_uint32), ("record_samples", C.c_uint32), ("collect_stats", C.c_uint32),
                 ("profile", C.c_uint32), ("megakernel", C.c_uint32), ("smem_levels", C.c_uint32),
                 ("ray_eps", C.c_float), ("refill_lanes", C.c_uint32), ("trace_steps", C.c_uint32),
-                ("bvh_width", C.c_uint32), ("bvh_cluster", C.c_uint32), ("bvh_collapse", C.c_uint32)]
+                ("bvh_width", C.c_uint32), ("bvh_cluster", C.c_uint32), ("bvh_collapse", C.c_uint32),
+                ("bvh_split", C.c_uint32)]
 
 
 class Q_cuda_stats(C.Structure):

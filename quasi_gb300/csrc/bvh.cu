@@ -137,6 +137,143 @@ __device__ __forceinline__ float3 centroid(float4 a, float4 b, float4 c) {
                __fmul_rn(__fadd_rn(__fadd_rn(a.z, b.z), c.z), third));
 }
 
+// ---------------------------------------------------------------- leaf references
+//
+// The hierarchy's leaves are references to triangles. Without splitting, reference i is
+// triangle i: its box is the bounds of its vertices and its Morton point is its centroid, bit
+// for bit as the oracle builds them. With splitting (Ernst and Greiner 2007, "Early split
+// clipping"), the S triangles whose boxes hold the most empty surface area are each cut in
+// two at the middle of their box's longest axis: reference i keeps triangle i with the bounds
+// of its part below the cut, reference n + k the part above it for the k-th of them. Every
+// reference carries a box that contains its part of the triangle, so together they cover the
+// whole triangle, and its Morton point is the centre of that box.
+
+struct RefView {
+    const uint32_t* tri = nullptr;  // reference -> triangle; null: reference i is triangle i
+    const float4* box = nullptr;    // 2 float4 per reference: (lo, -), (hi, -)
+};
+
+__device__ __forceinline__ void tri_bounds(float4 a, float4 b, float4 c, float3& lo, float3& hi) {
+    lo = mk3(fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z)));
+    hi = mk3(fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z)));
+}
+
+// Triangle of reference r and the reference's box.
+__device__ __forceinline__ uint32_t ref_geometry(const float4* __restrict__ tri_in, const RefView& rv, uint32_t r,
+                                                 float3& lo, float3& hi) {
+    if (!rv.tri) {
+        tri_bounds(__ldg(&tri_in[3 * r]), __ldg(&tri_in[3 * r + 1]), __ldg(&tri_in[3 * r + 2]), lo, hi);
+        return r;
+    }
+    const float4 l = __ldg(&rv.box[2 * r]), h = __ldg(&rv.box[2 * r + 1]);
+    lo = mk3(l.x, l.y, l.z);
+    hi = mk3(h.x, h.y, h.z);
+    return __ldg(&rv.tri[r]);
+}
+
+// Morton point of reference r: the triangle's centroid, or the centre of a split reference's box.
+__device__ __forceinline__ float3 ref_point(const float4* __restrict__ tri_in, const RefView& rv, uint32_t r) {
+    if (!rv.tri) return centroid(__ldg(&tri_in[3 * r]), __ldg(&tri_in[3 * r + 1]), __ldg(&tri_in[3 * r + 2]));
+    const float4 l = __ldg(&rv.box[2 * r]), h = __ldg(&rv.box[2 * r + 1]);
+    return mk3(__fmul_rn(__fadd_rn(l.x, h.x), 0.5f), __fmul_rn(__fadd_rn(l.y, h.y), 0.5f),
+               __fmul_rn(__fadd_rn(l.z, h.z), 0.5f));
+}
+
+// Sort key of triangle i for choosing the ones to split: the surface area of its box that
+// the triangle leaves empty, 2 (dx dy + dy dz + dz dx) - 2 area, as the bits of a non-negative
+// float (which order like the floats).
+__global__ void __launch_bounds__(256) k_split_keys(const float4* __restrict__ tri_in, uint32_t n,
+                                                    uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 a = __ldg(&tri_in[3 * i]), b = __ldg(&tri_in[3 * i + 1]), c = __ldg(&tri_in[3 * i + 2]);
+    float3 lo, hi;
+    tri_bounds(a, b, c, lo, hi);
+    const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+    const float3 e1 = mk3(b.x - a.x, b.y - a.y, b.z - a.z), e2 = mk3(c.x - a.x, c.y - a.y, c.z - a.z);
+    const float3 cr = cross(e1, e2);
+    const float empty = 2.0f * (dx * dy + dy * dz + dz * dx) - sqrtf(dot(cr, cr));
+    keys[i] = __float_as_uint(empty > 0.0f ? empty : 0.0f);
+    vals[i] = i;
+}
+
+// The part of triangle (a, b, c) on one side of the plane x_axis = cut (below: x <= cut):
+// the bounds of its vertices on that side and of the points where its edges cross the plane,
+// computed in FP64 and rounded outwards one float step beyond the directed rounding, so the
+// box contains the part whatever the rounding of the crossing points.
+__device__ void half_bounds(const float3 (&v)[3], int axis, float cut, bool below, float3& lo, float3& hi) {
+    double l[3] = {1e300, 1e300, 1e300}, h[3] = {-1e300, -1e300, -1e300};
+    auto grow = [&](double x, double y, double z) {
+        l[0] = fmin(l[0], x); l[1] = fmin(l[1], y); l[2] = fmin(l[2], z);
+        h[0] = fmax(h[0], x); h[1] = fmax(h[1], y); h[2] = fmax(h[2], z);
+    };
+    auto coord = [&](const float3& p) { return axis == 0 ? p.x : (axis == 1 ? p.y : p.z); };
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float3 p = v[k], q = v[(k + 1) % 3];
+        const float cp = coord(p), cq = coord(q);
+        if (below ? cp <= cut : cp >= cut) grow(p.x, p.y, p.z);
+        if ((cp < cut && cq > cut) || (cp > cut && cq < cut)) {
+            const double s = (static_cast<double>(cut) - cp) / (static_cast<double>(cq) - cp);
+            double x = p.x + s * (static_cast<double>(q.x) - p.x);
+            double y = p.y + s * (static_cast<double>(q.y) - p.y);
+            double z = p.z + s * (static_cast<double>(q.z) - p.z);
+            if (axis == 0) x = cut;
+            else if (axis == 1) y = cut;
+            else z = cut;
+            grow(x, y, z);
+        }
+    }
+    const float inf = __int_as_float(0x7f800000);
+    lo = mk3(nextafterf(__double2float_rd(l[0]), -inf), nextafterf(__double2float_rd(l[1]), -inf),
+             nextafterf(__double2float_rd(l[2]), -inf));
+    hi = mk3(nextafterf(__double2float_ru(h[0]), inf), nextafterf(__double2float_ru(h[1]), inf),
+             nextafterf(__double2float_ru(h[2]), inf));
+}
+
+// One thread per triangle in the order of k_split_keys' sort (ascending empty area): the last
+// s of them are split, the others become one reference each (see RefView).
+__global__ void __launch_bounds__(256) k_make_refs(const float4* __restrict__ tri_in, uint32_t n, uint32_t s,
+                                                   const uint32_t* __restrict__ sorted_tris,
+                                                   uint32_t* __restrict__ ref_tri, float4* __restrict__ ref_box) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const uint32_t t = sorted_tris[p];
+    const float4 a = __ldg(&tri_in[3 * t]), b = __ldg(&tri_in[3 * t + 1]), c = __ldg(&tri_in[3 * t + 2]);
+    float3 lo, hi;
+    tri_bounds(a, b, c, lo, hi);
+    ref_tri[t] = t;
+    if (p < n - s) {
+        ref_box[2 * t] = make_float4(lo.x, lo.y, lo.z, 0.f);
+        ref_box[2 * t + 1] = make_float4(hi.x, hi.y, hi.z, 0.f);
+        return;
+    }
+    const uint32_t r2 = n + (p - (n - s));
+    ref_tri[r2] = t;
+    const float ext[3] = {hi.x - lo.x, hi.y - lo.y, hi.z - lo.z};
+    const int axis = ext[0] >= ext[1] && ext[0] >= ext[2] ? 0 : (ext[1] >= ext[2] ? 1 : 2);
+    const float l = axis == 0 ? lo.x : (axis == 1 ? lo.y : lo.z), h = axis == 0 ? hi.x : (axis == 1 ? hi.y : hi.z);
+    const float cut = __fmul_rn(__fadd_rn(l, h), 0.5f);
+    float3 lo1 = lo, hi1 = hi, lo2 = lo, hi2 = hi;
+    if (cut > l && cut < h) {  // else (a box too thin to cut) both references keep the whole box
+        const float3 v[3] = {mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), mk3(c.x, c.y, c.z)};
+        half_bounds(v, axis, cut, true, lo1, hi1);
+        half_bounds(v, axis, cut, false, lo2, hi2);
+        // never beyond the triangle's own box, nor across the cut
+        lo1 = mk3(fmaxf(lo1.x, lo.x), fmaxf(lo1.y, lo.y), fmaxf(lo1.z, lo.z));
+        hi1 = mk3(fminf(hi1.x, hi.x), fminf(hi1.y, hi.y), fminf(hi1.z, hi.z));
+        lo2 = mk3(fmaxf(lo2.x, lo.x), fmaxf(lo2.y, lo.y), fmaxf(lo2.z, lo.z));
+        hi2 = mk3(fminf(hi2.x, hi.x), fminf(hi2.y, hi.y), fminf(hi2.z, hi.z));
+        if (axis == 0) { hi1.x = fminf(hi1.x, cut); lo2.x = fmaxf(lo2.x, cut); }
+        else if (axis == 1) { hi1.y = fminf(hi1.y, cut); lo2.y = fmaxf(lo2.y, cut); }
+        else { hi1.z = fminf(hi1.z, cut); lo2.z = fmaxf(lo2.z, cut); }
+    }
+    ref_box[2 * t] = make_float4(lo1.x, lo1.y, lo1.z, 0.f);
+    ref_box[2 * t + 1] = make_float4(hi1.x, hi1.y, hi1.z, 0.f);
+    ref_box[2 * r2] = make_float4(lo2.x, lo2.y, lo2.z, 0.f);
+    ref_box[2 * r2 + 1] = make_float4(hi2.x, hi2.y, hi2.z, 0.f);
+}
+
 __device__ __forceinline__ float warp_min(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -148,11 +285,11 @@ __device__ __forceinline__ float warp_max(float v) {
     return v;
 }
 
-__global__ void __launch_bounds__(256) k_bounds_partial(const float4* __restrict__ tri, uint32_t n,
+__global__ void __launch_bounds__(256) k_bounds_partial(const float4* __restrict__ tri, RefView rv, uint32_t n,
                                                         float* __restrict__ partial) {
     float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float3 c = centroid(__ldg(&tri[3 * i]), __ldg(&tri[3 * i + 1]), __ldg(&tri[3 * i + 2]));
+        const float3 c = ref_point(tri, rv, i);
         lo[0] = fminf(lo[0], c.x); lo[1] = fminf(lo[1], c.y); lo[2] = fminf(lo[2], c.z);
         hi[0] = fmaxf(hi[0], c.x); hi[1] = fmaxf(hi[1], c.y); hi[2] = fmaxf(hi[2], c.z);
     }
@@ -211,12 +348,12 @@ __device__ __forceinline__ uint32_t quantize10(float c, float lo, float inv) {
     return static_cast<uint32_t>(q);
 }
 
-__global__ void __launch_bounds__(256) k_morton(const float4* __restrict__ tri, uint32_t n,
+__global__ void __launch_bounds__(256) k_morton(const float4* __restrict__ tri, RefView rv, uint32_t n,
                                                 const float* __restrict__ bounds, uint32_t* __restrict__ morton,
                                                 uint32_t* __restrict__ keys, uint32_t* __restrict__ order) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float3 c = centroid(__ldg(&tri[3 * i]), __ldg(&tri[3 * i + 1]), __ldg(&tri[3 * i + 2]));
+    const float3 c = ref_point(tri, rv, i);
     const uint32_t qx = quantize10(c.x, bounds[0], bounds[6]);
     const uint32_t qy = quantize10(c.y, bounds[1], bounds[7]);
     const uint32_t qz = quantize10(c.z, bounds[2], bounds[8]);
@@ -270,14 +407,15 @@ __global__ void __launch_bounds__(256) k_karras(const uint32_t* __restrict__ key
 // One thread per leaf: gathers the triangle into leaf order and climbs to the root,
 // writing each child's box into its parent's slot. The second thread to arrive at a node
 // (arrival counter) owns the union and continues upwards.
-__global__ void __launch_bounds__(256) k_leaf_boxes(const float4* __restrict__ tri_in,
+__global__ void __launch_bounds__(256) k_leaf_boxes(const float4* __restrict__ tri_in, RefView rv,
                                                     const uint32_t* __restrict__ order, int n,
                                                     const int* __restrict__ parent, float4* nodes,
                                                     uint32_t* flags, float4* __restrict__ tris,
                                                     uint32_t* __restrict__ err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const uint32_t o = order[i];
+    float3 lo, hi;
+    const uint32_t o = ref_geometry(tri_in, rv, order[i], lo, hi);  // the reference's triangle and box
     const float4 a = __ldg(&tri_in[3 * o]), b = __ldg(&tri_in[3 * o + 1]), c = __ldg(&tri_in[3 * o + 2]);
     {
         // edges rounded to FP32, and the per-triangle factors of the test's error bound
@@ -289,8 +427,6 @@ __global__ void __launch_bounds__(256) k_leaf_boxes(const float4* __restrict__ t
         tris[3 * i + 1] = make_float4(e1.x, e1.y, e1.z, robust_k1(n1, n2));
         tris[3 * i + 2] = make_float4(e2.x, e2.y, e2.z, robust_k2(n1, n2));
     }
-    float3 lo = mk3(fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z)));
-    float3 hi = mk3(fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z)));
     if (n == 1) {
         nodes[0] = make_float4(lo.x, hi.x, lo.y, hi.y);
         nodes[1] = make_float4(lo.x, hi.x, lo.y, hi.y);
@@ -425,7 +561,7 @@ __device__ __forceinline__ void warp_box_scan(float (&lo)[3], float (&hi)[3], in
 }
 
 // One warp per subtree root from k_sah_roots.
-__global__ void __launch_bounds__(256) k_sah_rebuild(const float4* __restrict__ tri_in,
+__global__ void __launch_bounds__(256) k_sah_rebuild(const float4* __restrict__ tri_in, RefView rv,
                                                      const uint32_t* __restrict__ order, float4* nodes,
                                                      int* __restrict__ parent, int n_leaves,
                                                      const int* __restrict__ roots, const int* __restrict__ count,
@@ -463,14 +599,14 @@ __global__ void __launch_bounds__(256) k_sah_rebuild(const float4* __restrict__ 
         const bool have = lane < m;
         float lo[3], hi[3], ce[3];
         if (have) {
-            const uint32_t o = order[f + lane];
-            const float4 a = __ldg(&tri_in[3 * o]), b = __ldg(&tri_in[3 * o + 1]), c = __ldg(&tri_in[3 * o + 2]);
-            lo[0] = fminf(a.x, fminf(b.x, c.x));
-            lo[1] = fminf(a.y, fminf(b.y, c.y));
-            lo[2] = fminf(a.z, fminf(b.z, c.z));
-            hi[0] = fmaxf(a.x, fmaxf(b.x, c.x));
-            hi[1] = fmaxf(a.y, fmaxf(b.y, c.y));
-            hi[2] = fmaxf(a.z, fmaxf(b.z, c.z));
+            float3 l3, h3;
+            ref_geometry(tri_in, rv, order[f + lane], l3, h3);
+            lo[0] = l3.x;
+            lo[1] = l3.y;
+            lo[2] = l3.z;
+            hi[0] = h3.x;
+            hi[1] = h3.y;
+            hi[2] = h3.z;
 #pragma unroll
             for (int k = 0; k < 3; ++k) ce[k] = __fadd_rn(lo[k], hi[k]);
         } else {
@@ -1042,15 +1178,37 @@ void LbvhBuilder::release() {
     if (tree_) cudaFree(tree_);
     tree_ = nullptr;
     tree_n_ = tree_capacity_ = 0;
+    if (ref_tri_) cudaFree(ref_tri_);
+    if (ref_box_) cudaFree(ref_box_);
+    ref_tri_ = nullptr;
+    ref_box_ = nullptr;
+    ref_capacity_ = 0;
     radix_sort_release(sort_);
     capacity_ = 0;
     n_ = 0;
+    n_tris_ = 0;
+}
+
+cudaError_t LbvhBuilder::reserve_refs(uint32_t m) {
+    if (m <= ref_capacity_ && ref_tri_) return cudaSuccess;
+    if (ref_tri_) cudaFree(ref_tri_);
+    if (ref_box_) cudaFree(ref_box_);
+    ref_tri_ = nullptr;
+    ref_box_ = nullptr;
+    ref_capacity_ = 0;
+    QUASI_TRY_CUDA(cudaMalloc(&ref_tri_, sizeof(uint32_t) * m));
+    QUASI_TRY_CUDA(cudaMalloc(&ref_box_, sizeof(float4) * 2 * m));
+    ref_capacity_ = m;
+    return cudaSuccess;
 }
 
 cudaError_t LbvhBuilder::build(const float4* tri_in, uint32_t n, const int* emitters, uint32_t n_emit,
                                cudaStream_t stream, KernelProfiler& prof, uint32_t* err) {
-    QUASI_TRY_CUDA(reserve(n));
-    n_ = n;
+    // triangles split into two leaf references: a fixed share, so the leaf count is known here
+    const uint32_t split = n >= 4 ? static_cast<uint32_t>(uint64_t(n) * uint32_t(split_percent_) / 100u) : 0u;
+    QUASI_TRY_CUDA(reserve(n + split));
+    n_ = n + split;
+    n_tris_ = n;
     if (n == 0) return cudaSuccess;
     QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "tri_planes", stream,
                                 (k_tri_planes<<<ceil_div(n, 256), 256, 0, stream>>>(tri_in, n, tri_plane_))));
@@ -1066,14 +1224,28 @@ cudaError_t LbvhBuilder::build(const float4* tri_in, uint32_t n, const int* emit
                                     (k_emit_table<<<ceil_div(n_emit, 256), 256, 0, stream>>>(tri_in, emitters, n_emit,
                                                                                              emit_tab_))));
     }
+    RefView rv;
+    if (split > 0) {
+        QUASI_TRY_CUDA(reserve_refs(n + split));
+        // triangles in ascending order of the empty area of their boxes (keys_ and order_ are
+        // free until the Morton sort); the last `split` of them are cut
+        QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_split_keys", stream,
+                                    (k_split_keys<<<ceil_div(n, 256), 256, 0, stream>>>(tri_in, n, keys_, order_))));
+        QUASI_TRY_CUDA(radix_sort_pairs(keys_, order_, n, 32, sort_, stream, prof));
+        QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_make_refs", stream,
+                                    (k_make_refs<<<ceil_div(n, 256), 256, 0, stream>>>(tri_in, n, split, order_,
+                                                                                       ref_tri_, ref_box_))));
+        rv = RefView{ref_tri_, ref_box_};
+    }
+    n = n_;  // from here on the leaves
     const int parts = static_cast<int>(std::min<uint32_t>(k_bounds_blocks, ceil_div(n, 256)));
     QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_bounds", stream,
-                                (k_bounds_partial<<<parts, 256, 0, stream>>>(tri_in, n, partial_))));
+                                (k_bounds_partial<<<parts, 256, 0, stream>>>(tri_in, rv, n, partial_))));
     QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_bounds_final", stream,
                                 (k_bounds_final<<<1, 32, 0, stream>>>(partial_, parts, bounds_))));
     QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_morton", stream,
-                                (k_morton<<<ceil_div(n, 256), 256, 0, stream>>>(tri_in, n, bounds_, morton_, keys_,
-                                                                                order_))));
+                                (k_morton<<<ceil_div(n, 256), 256, 0, stream>>>(tri_in, rv, n, bounds_, morton_,
+                                                                                keys_, order_))));
     QUASI_TRY_CUDA(radix_sort_pairs(keys_, order_, n, 30, sort_, stream, prof));
     if (n > 1) {
         QUASI_TRY_CUDA(cudaMemsetAsync(flags_, 0, sizeof(uint32_t) * (n - 1), stream));
@@ -1083,7 +1255,7 @@ cudaError_t LbvhBuilder::build(const float4* tri_in, uint32_t n, const int* emit
     }
     QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_leaf_boxes", stream,
                                 (k_leaf_boxes<<<ceil_div(n, 256), 256, 0, stream>>>(
-                                    tri_in, order_, static_cast<int>(n), parent_, nodes_, flags_, tris_, err))));
+                                    tri_in, rv, order_, static_cast<int>(n), parent_, nodes_, flags_, tris_, err))));
     if (sah_cluster_ >= 3 && n >= 3) {
         QUASI_TRY_CUDA(cudaMemsetAsync(sah_count_, 0, sizeof(int), stream));
         QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_sah_roots", stream,
@@ -1092,7 +1264,7 @@ cudaError_t LbvhBuilder::build(const float4* tri_in, uint32_t n, const int* emit
         // at most one root per 3 leaves; 8 per block, a block per 24 leaves up to a full GPU
         const uint32_t blocks = std::max<uint32_t>(1, std::min<uint32_t>(ceil_div(n, 24), 152u * 8u));
         QUASI_TRY_CUDA(QUASI_LAUNCH(prof, "bvh_sah_rebuild", stream,
-                                    (k_sah_rebuild<<<blocks, 256, 0, stream>>>(tri_in, order_, nodes_, parent_,
+                                    (k_sah_rebuild<<<blocks, 256, 0, stream>>>(tri_in, rv, order_, nodes_, parent_,
                                                                                static_cast<int>(n), sah_roots_,
                                                                                sah_count_, err))));
     }

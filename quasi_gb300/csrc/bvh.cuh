@@ -11,6 +11,10 @@
 //   6. the 8-wide traversal records collapsed from the binary nodes (wide.cuh)
 //   7. per-triangle shading geometry: the unit normal of cross(e1, e2) and its length in
 //      double-float, read by every shading step instead of recomputing them
+// The leaves are references to triangles. By default the triangles whose boxes leave the
+// most surface area empty are first split in two (early split clipping, bvh.cu), so a scene
+// of n triangles has more than n leaves; with splitting off (set_split_percent(0)) leaf i
+// of the Morton order is a triangle and steps 1-5 are the oracle's, bit for bit.
 //
 // Node layout, 64 bytes (4 x float4), child boxes stored in the parent:
 //   n0 = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
@@ -44,10 +48,19 @@ void radix_sort_release(RadixSortScratch& s);
 cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t n, int key_bits,
                              RadixSortScratch& s, cudaStream_t stream, KernelProfiler& prof);
 
+// Percentage of a scene's triangles whose boxes are split in two before the hierarchy is
+// built (the ones whose boxes leave the most surface area empty). Benchmark frame (1M soup,
+// 1080p, 64 spp), Mrays/s by share: 0 %: 1539.3, 10 %: 1584.9, 20 %: 1593.7, 30 %: 1597.1,
+// 40 %: 1597.5, 50 %: 1592.5, 70 %: 1582.5 (triangle tests per closest-hit ray 5.54, 5.12,
+// 4.92, 4.77, 4.66, 4.57, 4.43; the build 2.4 ms at 0 %, 3.8 ms at 30 %).
+#ifndef QUASI_BVH_SPLIT_PERCENT
+#define QUASI_BVH_SPLIT_PERCENT 30
+#endif
+
 struct LbvhView {
     const float4* nodes = nullptr;  // 4 float4 per internal node
-    const float4* tris = nullptr;   // 3 float4 per triangle in leaf order
-    uint32_t tri_count = 0;
+    const float4* tris = nullptr;   // 3 float4 per leaf (triangle reference) in leaf order
+    uint32_t tri_count = 0;         // leaves
     uint32_t node_count = 0;
     const float4* tree = nullptr;   // top levels in breadth-first order (for shared memory)
     int tree_n = 0;                 // nodes in `tree`
@@ -80,6 +93,10 @@ public:
     // The 8-wide records' children from the surface-area-optimal spread (true) or by opening
     // the largest child greedily (false).
     void set_dp_collapse(bool on) { dp_collapse_ = on; }
+    // Percentage (0..100) of the triangles split into two leaf references before the build.
+    void set_split_percent(int p) { split_percent_ = p < 0 ? 0 : (p > 100 ? 100 : p); }
+    // Whether the last build split triangles (its leaves then outnumber the triangles).
+    bool split_active() const { return n_ != n_tris_; }
 
     // Copies the top max_nodes internal nodes (breadth first) for staging in shared memory.
     cudaError_t build_treelet(int max_nodes, cudaStream_t stream, KernelProfiler& prof);
@@ -96,7 +113,10 @@ public:
     cudaError_t read_wide(uint32_t* words, cudaStream_t stream) const;
 
 private:
-    uint32_t n_ = 0;
+    cudaError_t reserve_refs(uint32_t m);
+
+    uint32_t n_ = 0;                 // leaves (triangle references)
+    uint32_t n_tris_ = 0;            // triangles
     uint32_t capacity_ = 0;
     float* bounds_ = nullptr;        // 12 floats: lo.xyz hi.xyz inv.xyz pad
     float* partial_ = nullptr;       // per-block partial bounds
@@ -115,6 +135,10 @@ private:
     int* sah_roots_ = nullptr;       // roots of those subtrees
     int* sah_count_ = nullptr;
     bool dp_collapse_ = true;
+    int split_percent_ = QUASI_BVH_SPLIT_PERCENT;
+    uint32_t* ref_tri_ = nullptr;    // per reference: its triangle (split builds only)
+    float4* ref_box_ = nullptr;      // per reference: its box, 2 float4
+    uint32_t ref_capacity_ = 0;
     float* dp_cost_ = nullptr;       // 8 costs per internal node (k_collapse_dp)
     uint8_t* dp_dec_ = nullptr;      // 8 decisions per internal node
     float4* tree_ = nullptr;

@@ -108,7 +108,9 @@ __device__ __forceinline__ bool leaf_test(const float4* __restrict__ tris, const
     const float4* p = tris + 3ull * pos;
     const float4 a = __ldg(p), e1 = __ldg(p + 1), e2 = __ldg(p + 2);
     const int orig = __float_as_int(a.w);
-    if (orig == exclude) return false;
+    // (a triangle met again through another of its leaf references, split boxes, gives the
+    // same result as the first time: nothing to do if it is the closest hit already)
+    if (orig == exclude || orig == b.prim) return false;
     float t, dt;
     const int c = tri_classify<ANY>(r.o, r.d, a, e1, e2, t, dt);
     if (c == k_tri_miss) return false;
@@ -125,6 +127,7 @@ __device__ __forceinline__ bool leaf_test(const float4* __restrict__ tris, const
     if constexpr (ROBUST) {
         return redecide<ANY>(tri_in, xr, orig, b);
     } else {
+        if (b.undec == orig) return false;  // recorded through another leaf reference
         if (b.undec == k_undec_none) {
             b.undec = orig;
             return false;

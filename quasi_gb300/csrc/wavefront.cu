@@ -223,6 +223,13 @@ int Renderer::set_options(const Q_cuda_options& o) {
     if (n.bvh_cluster > 32) return fail(QUASI_ERR_INVALID, "bvh_cluster must be at most 32");
     if (n.bvh_cluster == 0) n.bvh_cluster = 32;
     if (n.bvh_collapse > 1) return fail(QUASI_ERR_INVALID, "bvh_collapse must be 0 or 1");
+    if (n.bvh_split > 100 && n.bvh_split != QUASI_BVH_SPLIT_NONE)
+        return fail(QUASI_ERR_INVALID, "bvh_split must be 0 (default), 1..100 or QUASI_BVH_SPLIT_NONE");
+    if (n.bvh_split == 0) n.bvh_split = QUASI_BVH_SPLIT_PERCENT == 0 ? QUASI_BVH_SPLIT_NONE : QUASI_BVH_SPLIT_PERCENT;
+    if (n.bvh_split != opt_.bvh_split) {
+        bvh_.set_split_percent(n.bvh_split == QUASI_BVH_SPLIT_NONE ? 0 : static_cast<int>(n.bvh_split));
+        bvh_dirty_ = true;
+    }
     if (n.bvh_collapse != opt_.bvh_collapse) {
         bvh_.set_dp_collapse(n.bvh_collapse == 0);
         bvh_dirty_ = true;
@@ -692,6 +699,7 @@ int Renderer::read_bvh(uint32_t* morton, uint32_t* order, int32_t* children, flo
               "lbvh build");
         bvh_dirty_ = false;
     }
+    if (bvh_.split_active()) return fail(QUASI_ERR_STATE, "the hierarchy has split references (bvh_split)");
     R_TRY(bvh_.read(morton, order, children, boxes, bounds, stream_), "read bvh");
     return QUASI_OK;
 }
@@ -704,6 +712,7 @@ int Renderer::read_wide_bvh(uint32_t* words) {
               "lbvh build");
         bvh_dirty_ = false;
     }
+    if (bvh_.split_active()) return fail(QUASI_ERR_STATE, "the hierarchy has split references (bvh_split)");
     R_TRY(bvh_.read_wide(words, stream_), "read wide bvh");
     return QUASI_OK;
 }

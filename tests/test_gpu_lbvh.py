@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 import quasi_gb300 as q
+from quasi_gb300 import _abi as A
 
 pytestmark = pytest.mark.gpu
 
@@ -15,8 +16,9 @@ pytestmark = pytest.mark.gpu
 @pytest.fixture(scope="module")
 def host(cuda_ok):
     h = q.PluginHost(width=32, height=32)
-    # the plain Morton hierarchy (no surface-area refinement), records by greedy opening
-    h.set_options(bvh_cluster=1, bvh_collapse=1)
+    # the plain Morton hierarchy over the triangles themselves (no split references, no
+    # surface-area refinement), records by greedy opening
+    h.set_options(bvh_cluster=1, bvh_collapse=1, bvh_split=A.QUASI_BVH_SPLIT_NONE)
     yield h
     h.destroy()
 

@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 import quasi_gb300 as q
+from quasi_gb300 import _abi as A
 from test_wide_oracle import _decode
 
 pytestmark = pytest.mark.gpu
@@ -54,6 +55,7 @@ def test_refined_hierarchy_is_valid_and_better(cuda_ok, orc, spec):
         scene = q.make_scene(spec, host.lib)
         n = scene.tri_count
         host.set_scene(scene)
+        host.set_options(bvh_split=A.QUASI_BVH_SPLIT_NONE)  # leaves = triangles, to compare them
         g = host.read_bvh(n)
         words = host.read_wide_bvh(n)
         assert host.stats().error_flags == 0
@@ -111,12 +113,13 @@ def test_refined_hierarchy_is_valid_and_better(cuda_ok, orc, spec):
     assert dp_cost <= greedy_cost * (1 + 1e-6), (dp_cost, greedy_cost)
 
 
-def _render(spec: str, cluster: int, collapse: int, w: int, h: int, spp: int, depth: int):
+def _render(spec: str, cluster: int, collapse: int, w: int, h: int, spp: int, depth: int,
+            split: int = A.QUASI_BVH_SPLIT_NONE):
     host = q.PluginHost(width=w, height=h)
     try:
         host.set_scene(q.make_scene(spec, host.lib))
         host.set_options(spp_per_frame=spp, max_depth=depth, seed=11, record_samples=1, collect_stats=1,
-                         bvh_cluster=cluster, bvh_collapse=collapse)
+                         bvh_cluster=cluster, bvh_collapse=collapse, bvh_split=split)
         host.render(w, h, dirty=True)
         img = np.array(host.readback())
         aov = host.readback_aov()
@@ -144,3 +147,43 @@ def test_refinement_leaves_images_identical(cuda_ok, spec, w, h, spp, depth):
         # plain + greedy opening
         visits = [r[3].node_visits for r in runs]
         assert visits[0] < visits[1] < visits[2], visits
+
+
+@pytest.mark.parametrize("spec,w,h,spp,depth", [("cornell36", 64, 48, 8, 4), ("soup:n=100000,seed=5", 160, 90, 8, 6)])
+def test_split_references_leave_images_identical(cuda_ok, spec, w, h, spp, depth):
+    """Early split clipping (bvh_split): the triangles whose boxes leave the most area empty
+    become two leaf references with the boxes of their halves. Every hit decision is exact,
+    so the frames over the split hierarchy (the default share, and half of the triangles)
+    equal those over the unsplit one bit for bit; on the soup the tighter leaf boxes mean
+    fewer triangle tests per ray."""
+    runs = [_render(spec, 0, 0, w, h, spp, depth, split) for split in (A.QUASI_BVH_SPLIT_NONE, 0, 50)]
+    a_img, a_aov, a_sig, a_st = runs[0]
+    for b_img, b_aov, b_sig, b_st in runs[1:]:
+        assert np.array_equal(a_img, b_img)
+        for k in a_aov:
+            assert np.array_equal(a_aov[k], b_aov[k]), k
+        assert np.array_equal(a_sig, b_sig)
+        assert (a_st.camera_rays, a_st.extension_rays, a_st.shadow_rays) == (b_st.camera_rays, b_st.extension_rays,
+                                                                             b_st.shadow_rays)
+    if spec.startswith("soup"):
+        tests = [r[3].tri_tests for r in runs]
+        assert tests[0] > tests[1] > tests[2], tests
+
+
+def test_split_hierarchy_is_not_read_back(cuda_ok):
+    """Q_cuda_read_bvh and Q_cuda_read_wide_bvh describe leaves that are triangles; over split
+    references they refuse with QUASI_ERR_STATE instead of returning arrays of another size."""
+    host = q.PluginHost(width=16, height=16)
+    try:
+        scene = q.make_scene("soup:n=1000,seed=1", host.lib)
+        host.set_scene(scene)
+        host.set_options(bvh_split=20)
+        with pytest.raises(q.QuasiError) as e1:
+            host.read_bvh(scene.tri_count)
+        with pytest.raises(q.QuasiError) as e2:
+            host.read_wide_bvh(scene.tri_count)
+        assert e1.value.code == A.QUASI_ERR_STATE and e2.value.code == A.QUASI_ERR_STATE
+        host.set_options(bvh_split=A.QUASI_BVH_SPLIT_NONE)
+        assert host.read_bvh(scene.tri_count)["order"].size == scene.tri_count
+    finally:
+        host.destroy()
