@@ -496,8 +496,8 @@ def run_ours(args) -> None:
                             "wave_spp": args.wave_spp, "trace_block": args.trace_block,
                             "refill_lanes": args.refill_lanes,
                             "bvh": ("binary LBVH" if args.bvh_width == 2 else "8-wide records collapsed from the LBVH")
-                                   + " (subtrees of <= 32 leaves rebuilt with the SAH split; records from the "
-                                     "SAH-optimal spread)"},
+                                   + " (30% of the triangles split into two leaf references; subtrees of <= 32 "
+                                     "leaves rebuilt with the SAH split; records from the SAH-optimal spread)"},
                 "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
                 "clocks": clocks.summary(), "batch": batch, "diff": diff}
         print(json.dumps(line), flush=True)

@@ -211,7 +211,8 @@ typedef struct Q_cuda_options {
                                     greedily */
     uint32_t bvh_split;          /* percentage of the triangles whose boxes are split in two
                                     leaf references before the LBVH is built, the ones whose
-                                    boxes leave the most surface area empty (0 = default 30;
+                                    boxes leave the most surface area empty, in scenes of at
+                                    least 131072 triangles (0 = default 30;
                                     1..100; QUASI_BVH_SPLIT_NONE = none: leaf i is the
                                     triangle at Morton position i, as the oracle builds it) */
 } Q_cuda_options;

@@ -1,7 +1,8 @@
-// bvh.cu - GPU LBVH construction: centroid bounds, Morton-30 codes, stable LSD radix sort,
-// Karras (2012) hierarchy and bottom-up child boxes. All FP32 arithmetic feeding integer
-// results uses round-to-nearest intrinsics so the compiler cannot contract it, which keeps
-// Morton codes, the sort order and the topology bit-exact against the oracle.
+// bvh.cu - GPU LBVH construction: leaf references (split triangle boxes), centroid bounds,
+// Morton-30 codes, stable LSD radix sort, Karras (2012) hierarchy and bottom-up child boxes.
+// All FP32 arithmetic feeding integer results uses round-to-nearest intrinsics so the
+// compiler cannot contract it, which keeps Morton codes, the sort order and the topology
+// bit-exact against the oracle when no triangle is split.
 #include "bvh.cuh"
 #include "common.cuh"
 #include "ffmath.cuh"
@@ -1205,7 +1206,8 @@ cudaError_t LbvhBuilder::reserve_refs(uint32_t m) {
 cudaError_t LbvhBuilder::build(const float4* tri_in, uint32_t n, const int* emitters, uint32_t n_emit,
                                cudaStream_t stream, KernelProfiler& prof, uint32_t* err) {
     // triangles split into two leaf references: a fixed share, so the leaf count is known here
-    const uint32_t split = n >= 4 ? static_cast<uint32_t>(uint64_t(n) * uint32_t(split_percent_) / 100u) : 0u;
+    const uint32_t split =
+        n >= k_split_min_tris ? static_cast<uint32_t>(uint64_t(n) * uint32_t(split_percent_) / 100u) : 0u;
     QUASI_TRY_CUDA(reserve(n + split));
     n_ = n + split;
     n_tris_ = n;

@@ -56,6 +56,10 @@ cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t n, int key
 #ifndef QUASI_BVH_SPLIT_PERCENT
 #define QUASI_BVH_SPLIT_PERCENT 30
 #endif
+// Scenes below this many triangles are not split: their builds are launch-bound, and the
+// split's key sort (13 more launches) cost the 10k-triangle soup's frame (512^2, 16 spp,
+// LBVH rebuilt every frame) 2.69 -> 2.82 ms, more than its traversal gained.
+constexpr uint32_t k_split_min_tris = 1u << 17;
 
 struct LbvhView {
     const float4* nodes = nullptr;  // 4 float4 per internal node
@@ -93,7 +97,8 @@ public:
     // The 8-wide records' children from the surface-area-optimal spread (true) or by opening
     // the largest child greedily (false).
     void set_dp_collapse(bool on) { dp_collapse_ = on; }
-    // Percentage (0..100) of the triangles split into two leaf references before the build.
+    // Percentage (0..100) of the triangles split into two leaf references before the build,
+    // in scenes of at least k_split_min_tris triangles.
     void set_split_percent(int p) { split_percent_ = p < 0 ? 0 : (p > 100 ? 100 : p); }
     // Whether the last build split triangles (its leaves then outnumber the triangles).
     bool split_active() const { return n_ != n_tris_; }

@@ -149,13 +149,14 @@ def test_refinement_leaves_images_identical(cuda_ok, spec, w, h, spp, depth):
         assert visits[0] < visits[1] < visits[2], visits
 
 
-@pytest.mark.parametrize("spec,w,h,spp,depth", [("cornell36", 64, 48, 8, 4), ("soup:n=100000,seed=5", 160, 90, 8, 6)])
+@pytest.mark.parametrize("spec,w,h,spp,depth", [("cornell36", 64, 48, 8, 4), ("soup:n=200000,seed=5", 160, 90, 8, 6)])
 def test_split_references_leave_images_identical(cuda_ok, spec, w, h, spp, depth):
-    """Early split clipping (bvh_split): the triangles whose boxes leave the most area empty
-    become two leaf references with the boxes of their halves. Every hit decision is exact,
-    so the frames over the split hierarchy (the default share, and half of the triangles)
-    equal those over the unsplit one bit for bit; on the soup the tighter leaf boxes mean
-    fewer triangle tests per ray."""
+    """Early split clipping (bvh_split): in scenes of at least 2^17 triangles, the triangles
+    whose boxes leave the most area empty become two leaf references with the boxes of their
+    halves. Every hit decision is exact, so the frames over the split hierarchy (the default
+    share, and half of the triangles) equal those over the unsplit one bit for bit; on the
+    200k soup the tighter leaf boxes mean fewer triangle tests per ray (the Cornell box is
+    below the size and stays unsplit)."""
     runs = [_render(spec, 0, 0, w, h, spp, depth, split) for split in (A.QUASI_BVH_SPLIT_NONE, 0, 50)]
     a_img, a_aov, a_sig, a_st = runs[0]
     for b_img, b_aov, b_sig, b_st in runs[1:]:
@@ -175,7 +176,7 @@ def test_split_hierarchy_is_not_read_back(cuda_ok):
     references they refuse with QUASI_ERR_STATE instead of returning arrays of another size."""
     host = q.PluginHost(width=16, height=16)
     try:
-        scene = q.make_scene("soup:n=1000,seed=1", host.lib)
+        scene = q.make_scene("soup:n=140000,seed=1", host.lib)
         host.set_scene(scene)
         host.set_options(bvh_split=20)
         with pytest.raises(q.QuasiError) as e1:
