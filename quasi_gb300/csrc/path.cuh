@@ -158,8 +158,8 @@ __device__ __forceinline__ float scene_entry(const float4* __restrict__ nodes, f
 // the binary LBVH; no shift when n_tris is 0): the error bound of an FP32 triangle test
 // grows with the distance from the ray's origin (robust.cuh), and camera rays otherwise
 // cross the empty space between the camera and the scene first. The shift te is kept in
-// lpath.w and added back to the first hit's t (the depth AOV); the stored double-float ray
-// keeps the camera origin.
+// lpath.w for the exact geometry of a re-decision (ExactShifted); the stored double-float ray
+// keeps the camera origin, from which shading measures the first hit's depth.
 __device__ __forceinline__ bool begin_path(const FrameParams& f, const PathDev& p, uint32_t pid, uint32_t local,
                                            const float4* __restrict__ nodes, uint32_t n_tris, float3& o, float3& d) {
     const uint32_t j = local / f.slots;
@@ -347,13 +347,14 @@ __device__ __forceinline__ void shade_and_enqueue(bool active, const FrameParams
         const float3 alb = xyz(__ldg(&s.albedo[prim]));
         nb = bounce == 1 ? alb : xyz(p.beta[pid]) * alb;  // beta is 1 at the first hit (1 * a = a)
         cont = bounce < f.max_depth && max3(nb) > 0.0f;
-        vertex_point(vs, prim, ro, rd, x, nrm);
+        float t_hit;
+        vertex_point(vs, prim, ro, rd, x, nrm, t_hit);
         org = vertex_origin(vs, x, nrm);
         if (bounce == 1) {
             const float3 em = xyz(__ldg(&s.emission[prim]));
-            const float te = p.lpath[pid].w;  // the camera ray's FP32 start shift (begin_path)
             p.lpath[pid] = make_float4(em.x, em.y, em.z, 0.f);
-            first_hit_aovs(alb, em, h.x + te, ff3_f(nrm), p.aov_a[pid], p.aov_n[pid]);
+            // the depth from the camera: the plane's t along the (unshifted) double-float ray
+            first_hit_aovs(alb, em, t_hit, ff3_f(nrm), p.aov_a[pid], p.aov_n[pid]);
         }
         p.beta[pid] = make_float4(nb.x, nb.y, nb.z, 0.f);
     }
@@ -477,7 +478,7 @@ __device__ __forceinline__ float3 trace_path(const FrameParams& f, const SceneDe
         if (k == 1) {
             const float3 em = xyz(__ldg(&s.emission[prim]));
             L = em;
-            if (aov_a) first_hit_aovs(alb, em, t, v.nrm, *aov_a, *aov_n);
+            if (aov_a) first_hit_aovs(alb, em, v.t, v.nrm, *aov_a, *aov_n);
         }
         float gv = 0.0f;
         if (v.nee) {

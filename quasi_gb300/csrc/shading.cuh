@@ -40,6 +40,7 @@ struct VertexResult {
     ff3 seg_o, seg_d;  // the exact shadow segment: start and end - start (double-float)
     ff3 org;           // continuation origin x + eps n (double-float)
     ff3 dir;           // continuation direction (valid when want_dir)
+    float t;           // distance of the hit along the ray (the plane's, rounded to float)
 };
 
 // FP32 dot product with a fixed operation order (no contraction choices left to the
@@ -92,18 +93,24 @@ __device__ __forceinline__ LightTri load_light(const VertexScene& s, uint32_t se
 
 // The hit point x (the hit triangle's plane n.x = n.v0 intersected with the double-float ray
 // ro + t rd, t = (n.v0 - n.ro) / n.rd) and the unit normal facing the ray.
+// t_hit: the hit's distance along the ray, the plane's t rounded to float (the first-hit
+// depth). It depends only on the ray and the triangle, whereas the traversal's t depends on
+// whether the hit was decided by the FP32 test or re-decided exactly, and so on the order in
+// which a hierarchy presents the candidates.
 __device__ __forceinline__ void vertex_point(const VertexScene& s, int prim, const ff3& ro, const ff3& rd, ff3& x,
-                                             ff3& nrm) {
+                                             ff3& nrm, float& t_hit) {
     const float4 p = __ldg(&s.tri_plane[2 * prim]), q = __ldg(&s.tri_plane[2 * prim + 1]);
     nrm = ff3{ff{p.x, p.y}, ff{p.z, p.w}, ff{q.x, q.y}};
     const ff den = ff3_dot_fast(nrm, rd);
     if (den.hi != 0.0f) {
         const ff t = ff_div(ff_sub_fast(ff{q.z, q.w}, ff3_dot_fast(nrm, ro)), den);
         x = ff3_add_fast(ro, ff3_scale(rd, t));
+        t_hit = ff_f(t);
     } else {
         // A ray parallel to the plane cannot hit the triangle (an exact hit needs
         // det = -d.(e1 x e2) != 0); kept only so that x is defined.
         x = ro;
+        t_hit = 0.0f;
     }
     if (den.hi > 0.0f) nrm = ff3_neg(nrm);
 }
@@ -207,7 +214,7 @@ __device__ __forceinline__ void shade_vertex(const VertexScene& s, uint32_t key,
     const VertexRandom r = vertex_random(key);
     const LightTri lt = load_light(s, r.sel);
     ff3 x, nrm;
-    vertex_point(s, prim, ro, rd, x, nrm);
+    vertex_point(s, prim, ro, rd, x, nrm, out.t);
     out.nrm = ff3_f(nrm);
     out.org = vertex_origin(s, x, nrm);
     vertex_light(s, prim, lt, r.r1, r.r2, x, nrm, out.org, out);
