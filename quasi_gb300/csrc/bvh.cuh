@@ -57,8 +57,8 @@ cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t n, int key
 #define QUASI_BVH_SPLIT_PERCENT 30
 #endif
 // Scenes below this many triangles are not split: their builds are launch-bound, and the
-// split's key sort (13 more launches) cost the 10k-triangle soup's frame (512^2, 16 spp,
-// LBVH rebuilt every frame) 2.69 -> 2.82 ms, more than its traversal gained.
+// split's key sort and references (14 more launches) cost the 10k-triangle soup's frame
+// (512^2, 16 spp, LBVH rebuilt every frame) 2.69 -> 2.82 ms, more than its traversal gained.
 constexpr uint32_t k_split_min_tris = 1u << 17;
 
 struct LbvhView {
